@@ -1,0 +1,451 @@
+"""Benchmark of the grid2grid transform path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+                    [--impl ours|reference]
+
+Workload (default): random_grid_f32_16384 -- float 16384 x 16384 redistributed
+between two arbitrary grid-like layouts over 16 virtual ranks (random split
+points with extents U[1, 2048], random owners, every block separately
+allocated with a padded stride), seeded random bit patterns.
+
+A step is one transform of that matrix. `value` is redistributed GB/s
+(m*n*sizeof(T) per step / time) with the layouts resident in HBM and the plan
+cached: the device-timed gather-scatter. `e2e` is the same metric through the
+host-buffer call a CPU caller makes: host-to-device copy of the initial
+layout from pinned memory, plan + transform (the reference's transform also
+re-plans every call), device-to-host copy of the final layout.
+
+`--impl reference` times the reference algorithm on the host cores (the
+reference library itself where it was built for this host, else the
+project's CPU restatement of it) on the same workload and prints the same
+line with "impl": "reference".
+
+Multi-GPU: the transform does not shard across GPUs here (no cross-GPU
+exchange is built): each rank runs an independent replica, `value` is the sum
+over ranks, timing is max over ranks ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "redistributed GB/s"
+UNIT = "GB/s"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _profile_traffic(kernel: str, workload: str):
+    """dram bytes per launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"dram_bytes_per_launch\s*=\s*([0-9]+)", open(p).read())
+    return int(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled in the background."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int, period_ms: int = 20):
+        self.index = index
+        self.period = period_ms
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", f"-lms={self.period}"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        t0 = time.time()
+        while not self.samples and time.time() - t0 < 3.0:
+            time.sleep(0.01)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        win = [p for (t, p) in self.samples if t0 - 0.05 <= t <= t1 + 0.05]
+        if not win:
+            win = [p for (_, p) in self.samples[-3:]]
+        if not win:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"],
+                    "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(p[1]) for p in win if num(p[1]) is not None]
+        mx = [num(p[2]) for p in win if num(p[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for p in win for k in range(4)
+                          if p[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(win)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _allreduce_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def time_cpu_reference(w, reps: int, threads: int, host_arenas=None):
+    """Times the reference algorithm on the host: the reference library when it
+    was built for this host (oracle/_ref), else the oracle port. Returns
+    (seconds per transform list, kind, sample description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from grid2grid_gb300 import workloads as W
+    if host_arenas is None:
+        ia, fa = W.fill_arenas(w)
+    else:
+        ia, fa = host_arenas
+    kind = "port"
+    use_ref = False
+    if oracle.ref_available() and len({L.dtype for L in w.inits}) == 1:
+        try:
+            oracle.ref()
+            use_ref = True
+            kind = "reference"
+        except OSError:
+            use_ref = False
+    if not use_ref:
+        oracle.build_port()
+    times = []
+    ops = None if w.ops is None else list(w.ops)
+    from grid2grid_gb300 import capi
+    for r in range(reps + 1):
+        fcopy = [a.copy() for a in fa]
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_transform(w.inits, w.finals, ia, fcopy,
+                                 None if ops is None else [capi.make_op(*o) for o in ops],
+                                 oracle.MODE_SINGLE_SCALED if ops else oracle.MODE_SINGLE)
+        else:
+            oracle.port_transform(w.inits, w.finals, ia, fcopy, ops, threads=threads)
+        dt = time.perf_counter() - t0
+        if r > 0:  # first run warms page tables and caches
+            times.append(dt)
+    ranks = max(L.n_ranks for L in w.inits + w.finals)
+    sample = (f"{w.name}: full transform x{reps} after 1 warm-up; "
+              f"{ranks} ranks as {'thread-MPI ranks' if use_ref else 'threads'}"
+              f" on {threads} host threads")
+    return times, kind, sample
+
+
+def run_reference_arm(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from grid2grid_gb300 import workloads as W
+    w = W.BY_NAME[args.workload]()
+    threads = _cpu_threads()
+    reps = max(1, args.steps)
+    times, kind, sample = time_cpu_reference(w, reps + max(0, args.warmup - 1), threads)
+    times = times[-reps:]
+    sec = statistics.median(times)
+    value = w.bytes_moved / sec / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "impl": "reference",
+        "n_gpus": args.gpus, "steps": reps, "warmup": args.warmup,
+        "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": _dtype_name(w), "data": "synthetic (seeded)",
+        "config": _config(w, args),
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
+                         "kind": kind, "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _dtype_name(w):
+    from grid2grid_gb300 import capi
+    names = sorted({capi.DTYPE_NAME[L.dtype] for L in w.inits})
+    short = {"float32": "f32", "float64": "f64", "complex64": "c64", "complex128": "c128"}
+    return "+".join(short[n] for n in names)
+
+
+def _config(w, args):
+    c = {"workload": w.name}
+    c.update(w.meta)
+    c["bytes_per_step"] = w.bytes_moved
+    c["l2"] = "inputs larger than L2 (no flush)" if w.bytes_moved > 256 * 2**20 else \
+        "L2 flushed between steps"
+    c["parallelism"] = f"replicas x{args.gpus}"
+    return c
+
+
+def run_ours(args):
+    import torch
+    from grid2grid_gb300 import capi
+    from grid2grid_gb300 import workloads as W
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = capi.load()
+    w = W.BY_NAME[args.workload]()
+    dev = torch.device("cuda", local)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    dev_i = [torch.randint(0, 256, (L.arena_bytes,), dtype=torch.uint8, device=dev,
+                           generator=gen) for L in w.inits]
+    dev_f = [torch.randint(0, 256, (L.arena_bytes,), dtype=torch.uint8, device=dev,
+                           generator=gen) for L in w.finals]
+    keep = []
+
+    def descs(layouts, tensors):
+        arr = (capi.LayoutDesc * len(layouts))()
+        for k, (L, t) in enumerate(zip(layouts, tensors)):
+            d, kk = L.desc(t.data_ptr())
+            arr[k] = d
+            keep.append(kk)
+        return arr
+
+    n = len(w.inits)
+    dI, dF = descs(w.inits, dev_i), descs(w.finals, dev_f)
+    dts = (C.c_int * n)(*w.dtypes())
+    ops = None
+    if w.ops is not None:
+        ops = (capi.Op * n)(*[capi.make_op(*o) for o in w.ops])
+    stream = torch.cuda.Stream(device=dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    plan = C.c_void_p()
+    t_plan0 = time.perf_counter()
+    capi.check(lib.g2g_plan_create_batch(n, dI, dF, dts, ops, sp, C.byref(plan)))
+    plan_ms = (time.perf_counter() - t_plan0) * 1e3
+    tuned = None
+    if args.autotune:
+        t = capi.Tuning()
+        capi.check(lib.g2g_plan_autotune(plan, sp, 3, C.byref(t)))
+        tuned = {k: getattr(t, k) for k in ("tile_bytes", "tile_dim", "ctas_per_sm",
+                                            "threads", "unroll")}
+    info = capi.PlanInfo()
+    capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
+    # warm-up
+    for _ in range(args.warmup):
+        capi.check(lib.g2g_plan_execute(plan, sp))
+    stream.synchronize()
+    sampler = ClockSampler(local).start() if rank == 0 else None
+    # timed region: one launch per step, events around each launch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    _barrier(ws)
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    start_all = torch.cuda.Event(enable_timing=True)
+    end_all = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        start_all.record(stream)
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            capi.check(lib.g2g_plan_execute(plan, sp))
+            ev[k][1].record(stream)
+        end_all.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    _barrier(ws)
+    t_wall1 = time.time()
+    total_ms = start_all.elapsed_time(end_all)
+    launch_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = _allreduce_max(total_ms, ws)
+    ms_per_step = total_ms / args.steps
+    kernel_ms = statistics.mean(launch_ms)
+    clocks = None
+    if sampler is not None:
+        time.sleep(0.06)
+        sampler.stop()
+        clocks = sampler.summary(t_wall0, t_wall1)
+    bytes_step = info.bytes_moved
+    value = bytes_step * ws / (ms_per_step * 1e-3) / 1e9
+    peak, peak_kind = _peaks()
+    achieved = info.bytes_min_traffic / (kernel_ms * 1e-3) / 1e9
+    traffic = _profile_traffic("g2g_scatter", w.name)
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": info.bytes_min_traffic,
+                "kernel_ms": round(kernel_ms, 5)}
+
+    # e2e: host buffers through the host-layout call, copies inside the timing
+    e2e = None
+    if args.e2e_steps > 0:
+        e2e = run_e2e(lib, w, dev_i, dev_f, args.e2e_steps, stream, ws)
+    capi.check(lib.g2g_plan_destroy(plan))
+
+    cpu = None
+    if rank == 0 and ws == 1 and args.cpu_reps > 0:
+        host_i = [t.cpu().numpy() for t in dev_i]
+        host_f = [t.cpu().numpy() for t in dev_f]
+        threads = _cpu_threads()
+        times, kind, sample = time_cpu_reference(w, args.cpu_reps, threads,
+                                                 (host_i, host_f))
+        sec = statistics.median(times)
+        cpu = {"value": round(w.bytes_moved / sec / 1e9, 4), "unit": UNIT,
+               "cores": threads, "kind": kind, "sample": sample}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_per_step, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": _dtype_name(w),
+            "data": "synthetic (seeded random bit patterns, device-resident)",
+            "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
+            "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
+                     "create_ms": round(plan_ms, 3), "autotuned": tuned,
+                     "tuning": {k: getattr(info.tuning, k) for k in
+                                ("tile_bytes", "tile_dim", "ctas_per_sm", "threads",
+                                 "unroll")}},
+        }
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
+    """Host-buffer transform: H2D of the initial layout's arena from pinned
+    memory, one-shot plan + transform, D2H of the final layout's arena. The
+    device copy of the final arena mirrors the host one (same padding bytes),
+    so copying it back leaves the host padding unchanged."""
+    import torch
+    from grid2grid_gb300 import capi
+    host_i = [t.cpu().pin_memory() for t in dev_i]
+    host_f = [t.cpu().pin_memory() for t in dev_f]
+    n = len(w.inits)
+    keep = []
+
+    def descs(layouts, tensors):
+        arr = (capi.LayoutDesc * len(layouts))()
+        for k, (L, t) in enumerate(zip(layouts, tensors)):
+            d, kk = L.desc(t.data_ptr())
+            arr[k] = d
+            keep.append(kk)
+        return arr
+    dI, dF = descs(w.inits, dev_i), descs(w.finals, dev_f)
+    dts = (C.c_int * n)(*w.dtypes())
+    ops = None
+    if w.ops is not None:
+        ops = (capi.Op * n)(*[capi.make_op(*o) for o in w.ops])
+    sp = C.c_void_p(stream.cuda_stream)
+    h2d = sum(t.numel() for t in host_i)
+    d2h = sum(t.numel() for t in host_f)
+
+    def step():
+        with torch.cuda.stream(stream):
+            for d, h in zip(dev_i, host_i):
+                d.copy_(h, non_blocking=True)
+        capi.check(lib.g2g_transform_batch(n, dI, dF, dts, ops, sp))
+        with torch.cuda.stream(stream):
+            for d, h in zip(dev_f, host_f):
+                h.copy_(d, non_blocking=True)
+        stream.synchronize()
+    step()  # warm-up
+    _barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t = (time.perf_counter() - t0) / steps
+    t = _allreduce_max(t, ws)
+    return {"value": round(w.bytes_moved * ws / t / 1e9, 3), "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": round(t * 1e3, 3), "steps": steps,
+            "path": "pinned host arenas -> g2g_transform_batch (plan+execute) -> host"}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="random_grid_f32_16384")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-reps", type=int, default=2)
+    ap.add_argument("--autotune", action="store_true")
+    args = ap.parse_args(argv)
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,917 @@
+// Host side of the C ABI (include/grid2grid_gb300.h): descriptor validation,
+// the dense block tables, plan lifetime, execution, graph capture, tuning.
+//
+// Validation turns every condition under which the reference throws
+// (interval.cpp:5-17, grid2D.cpp:29-43, block.cpp:167-174,
+// grid_cover.hpp:57-62) or asserts (communication_data.cpp:227-239,
+// grid_cover.cpp:70, grid2D.cpp:117) -- or silently hangs in MPI because a
+// block is not held by its owner -- into G2G_ERROR_INVALID_ARGUMENT with a
+// message, before any device work is queued.
+#include "../../include/grid2grid_gb300.h"
+#include "g2g_internal.hpp"
+#include "g2g_launch.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cctype>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string t_last_error;
+
+g2g_status fail(g2g_status st, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+    return st;
+}
+
+#define G2G_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return fail(e_ == cudaErrorMemoryAllocation ? G2G_ERROR_OUT_OF_MEMORY       \
+                                                        : G2G_ERROR_CUDA,               \
+                        "CUDA error %s (%s) at %s:%d", cudaGetErrorName(e_),            \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                    \
+    } while (0)
+
+#define G2G_TRY(expr)                                                                   \
+    do {                                                                                \
+        g2g_status s_ = (expr);                                                         \
+        if (s_ != G2G_SUCCESS)                                                          \
+            return s_;                                                                  \
+    } while (0)
+
+int dtype_esz(int dt) {
+    switch (dt) {
+    case G2G_FLOAT32: return 4;
+    case G2G_FLOAT64: return 8;
+    case G2G_COMPLEX64: return 8;
+    case G2G_COMPLEX128: return 16;
+    default: return 0;
+    }
+}
+uint32_t esz_code(int esz) { return esz == 4 ? 0u : esz == 8 ? 1u : 2u; }
+bool dtype_complex(int dt) { return dt == G2G_COMPLEX64 || dt == G2G_COMPLEX128; }
+
+// --------------------------------------------------------------- per device
+struct DeviceState {
+    int sm_count = 0;
+    cudaStream_t plan_stream = nullptr;
+    // Pinned staging for plan uploads; planning holds `mu` from the upload
+    // to the synchronisation that ends it, so one buffer serves all plans.
+    std::mutex mu;
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+};
+std::mutex g_dev_mu;
+std::map<int, DeviceState> g_devices;
+
+g2g_status device_state(DeviceState **out, int *dev_out) {
+    int dev = 0;
+    G2G_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    DeviceState &ds = g_devices[dev];
+    if (!ds.plan_stream) {
+        G2G_CUDA(cudaDeviceGetAttribute(&ds.sm_count, cudaDevAttrMultiProcessorCount, dev));
+        G2G_CUDA(cudaStreamCreateWithFlags(&ds.plan_stream, cudaStreamNonBlocking));
+    }
+    *out = &ds;
+    if (dev_out)
+        *dev_out = dev;
+    return G2G_SUCCESS;
+}
+
+// ------------------------------------------------------------ host layouts
+struct HBlock {
+    int rank, row, col;
+    bool trans, conj;
+    int64_t stride;
+    uint64_t data;
+};
+
+struct HLayout {
+    std::vector<int32_t> rs, cs, owners;
+    std::vector<int32_t> reo;
+    int n_ranks = 0;
+    std::vector<HBlock> blocks;
+    int nbr() const { return (int)rs.size() - 1; }
+    int nbc() const { return (int)cs.size() - 1; }
+    int owner(int i, int j) const {
+        int r = owners[(size_t)i * nbc() + j];
+        return reo.empty() ? r : reo[r];
+    }
+};
+
+g2g_status check_splits(const int32_t *s, int n, const char *what, const char *which) {
+    if (n < 0)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout: negative number of %s blocks",
+                    which, what);
+    if (!s)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout: %s_split is NULL", which, what);
+    for (int i = 0; i <= n; ++i) {
+        if (s[i] < 0)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: %s_split[%d] = %d is negative (interval bounds must be "
+                        ">= 0)",
+                        which, what, i, s[i]);
+        if (i && s[i] < s[i - 1])
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: %s_split is decreasing at index %d (%d > %d); "
+                        "intervals need start <= end",
+                        which, what, i, s[i - 1], s[i]);
+    }
+    return G2G_SUCCESS;
+}
+
+// Reads and validates one layout descriptor. `P` is the number of virtual
+// ranks of the transform (the communicator size).
+g2g_status load_layout(const g2g_layout_desc *d, const char *which, int P, bool is_final,
+                       HLayout &L) {
+    if (!d)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout descriptor is NULL", which);
+    G2G_TRY(check_splits(d->rows_split, d->n_block_rows, "rows", which));
+    G2G_TRY(check_splits(d->cols_split, d->n_block_cols, "cols", which));
+    const int nbr = d->n_block_rows, nbc = d->n_block_cols;
+    L.rs.assign(d->rows_split, d->rows_split + nbr + 1);
+    L.cs.assign(d->cols_split, d->cols_split + nbc + 1);
+    L.n_ranks = d->n_ranks;
+    if (d->n_ranks < 0)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout: negative n_ranks", which);
+    const size_t nblk = (size_t)nbr * (size_t)nbc;
+    if (nblk && !d->owners)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout: owners is NULL", which);
+    L.owners.assign(d->owners, d->owners + nblk);
+    if (d->n_reordering < 0 || (d->n_reordering > 0 && !d->reordering))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout: bad rank reordering", which);
+    if (d->n_reordering > 0) {
+        L.reo.assign(d->reordering, d->reordering + d->n_reordering);
+        for (int r : L.reo)
+            if (r < 0 || r >= P)
+                return fail(G2G_ERROR_INVALID_ARGUMENT,
+                            "%s layout: reordering maps to rank %d outside [0, %d)", which,
+                            r, P);
+    }
+    const int owner_limit =
+        L.reo.empty() ? d->n_ranks : std::max((int)L.reo.size(), d->n_ranks);
+    for (size_t k = 0; k < nblk; ++k) {
+        int o = L.owners[k];
+        if (o < 0 || o >= owner_limit || (!L.reo.empty() && o >= (int)L.reo.size()))
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: block (%d, %d) has owner %d outside [0, %d)", which,
+                        (int)(k / (size_t)std::max(nbc, 1)), (int)(k % (size_t)std::max(nbc, 1)),
+                        o, owner_limit);
+        if (L.reo.empty() && o >= P)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: owner %d is not a rank of the transform (%d ranks)",
+                        which, o, P);
+    }
+    if (d->n_blocks < 0 || (d->n_blocks > 0 && !d->blocks))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout: bad local block list", which);
+    std::vector<char> seen(nblk, 0);
+    L.blocks.resize(d->n_blocks);
+    for (int b = 0; b < d->n_blocks; ++b) {
+        const g2g_block_desc &bd = d->blocks[b];
+        if (bd.rank < 0 || bd.rank >= P)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: local block %d belongs to rank %d outside [0, %d)", which,
+                        b, bd.rank, P);
+        if (bd.row < 0 || bd.row >= nbr || bd.col < 0 || bd.col >= nbc)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: local block %d has coordinates (%d, %d) outside the "
+                        "%d x %d grid",
+                        which, b, bd.row, bd.col, nbr, nbc);
+        size_t idx = (size_t)bd.row * nbc + bd.col;
+        if (seen[idx])
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: block (%d, %d) is listed more than once", which, bd.row,
+                        bd.col);
+        seen[idx] = 1;
+        int own = L.owner(bd.row, bd.col);
+        if (own != bd.rank)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: block (%d, %d) is held by rank %d but owned by rank %d",
+                        which, bd.row, bd.col, bd.rank, own);
+        if (is_final && bd.transpose_on_copy)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "final layout: block (%d, %d) is marked transpose_on_copy; a "
+                        "destination block cannot be transposed",
+                        bd.row, bd.col);
+        const int64_t nr = L.rs[bd.row + 1] - L.rs[bd.row];
+        const int64_t nc = L.cs[bd.col + 1] - L.cs[bd.col];
+        const int64_t srows = bd.transpose_on_copy ? nc : nr; // storage rows
+        const int64_t scols = bd.transpose_on_copy ? nr : nc;
+        if (nr > 0 && nc > 0) {
+            if (!bd.data)
+                return fail(G2G_ERROR_INVALID_ARGUMENT,
+                            "%s layout: block (%d, %d) has a NULL data pointer", which,
+                            bd.row, bd.col);
+            if (bd.stride < 1 || (scols > 1 && bd.stride < srows))
+                return fail(G2G_ERROR_INVALID_ARGUMENT,
+                            "%s layout: block (%d, %d) has stride %lld < %lld stored rows",
+                            which, bd.row, bd.col, (long long)bd.stride, (long long)srows);
+        }
+        HBlock hb;
+        hb.rank = bd.rank;
+        hb.row = bd.row;
+        hb.col = bd.col;
+        hb.trans = bd.transpose_on_copy != 0;
+        hb.conj = hb.trans && bd.conjugate_on_copy != 0; // conj acts only with transpose
+        hb.stride = bd.stride;
+        hb.data = (uint64_t)(uintptr_t)bd.data;
+        L.blocks[b] = hb;
+    }
+    for (size_t k = 0; k < nblk; ++k)
+        if (!seen[k]) {
+            int i = (int)(k / (size_t)nbc), j = (int)(k % (size_t)nbc);
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: block (%d, %d) owned by rank %d is missing from that "
+                        "rank's local blocks",
+                        which, i, j, L.owner(i, j));
+        }
+    return G2G_SUCCESS;
+}
+
+// grid_layout::transpose_or_conjugate (grid_layout.hpp:18-25): transposes the
+// grid and the owners and marks every block (block.cpp:249-288).
+void transpose_layout(HLayout &L, char flag) {
+    if (flag != 'T' && flag != 'C')
+        return;
+    const int nbr = L.nbr(), nbc = L.nbc();
+    std::vector<int32_t> t((size_t)nbr * nbc);
+    for (int i = 0; i < nbr; ++i)
+        for (int j = 0; j < nbc; ++j)
+            t[(size_t)j * nbr + i] = L.owners[(size_t)i * nbc + j];
+    L.owners.swap(t);
+    std::swap(L.rs, L.cs);
+    for (HBlock &b : L.blocks) {
+        std::swap(b.row, b.col);
+        b.trans = true;
+        if (flag == 'C')
+            b.conj = true;
+    }
+}
+
+// ------------------------------------------------------------------- plans
+struct PairHost {
+    HLayout a, b; // a: initial after op, b: final
+    int dtype = 0;
+    int esz = 0;
+    bool scaled = false;
+    bool any_trans = false;
+    double alpha[2] = {1, 0}, beta[2] = {0, 0};
+    int64_t m = 0, n = 0;
+};
+
+g2g_tuning default_tuning() {
+    g2g_tuning t;
+    std::memset(&t, 0, sizeof(t));
+    t.tile_bytes = 32 * 1024;
+    t.tile_dim = 32;
+    t.ctas_per_sm = 4;
+    t.threads = 256;
+    t.unroll = 4;
+    return t;
+}
+
+g2g_tuning merge_tuning(const g2g_tuning &base, const g2g_tuning *over) {
+    g2g_tuning t = base;
+    if (!over)
+        return t;
+    if (over->tile_bytes) t.tile_bytes = over->tile_bytes;
+    if (over->tile_dim) t.tile_dim = over->tile_dim;
+    if (over->ctas_per_sm) t.ctas_per_sm = over->ctas_per_sm;
+    if (over->threads) t.threads = over->threads;
+    if (over->unroll) t.unroll = over->unroll;
+    return t;
+}
+
+g2g_status check_tuning(const g2g_tuning &t) {
+    if (t.tile_bytes < 512 || t.tile_bytes > (1 << 24))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_bytes %d outside [512, 16M]",
+                    t.tile_bytes);
+    if (t.tile_dim != 16 && t.tile_dim != 32 && t.tile_dim != 64)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_dim must be 16, 32 or 64");
+    if (t.threads != 128 && t.threads != 256 && t.threads != 512)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: threads must be 128, 256 or 512");
+    if (t.unroll != 1 && t.unroll != 2 && t.unroll != 4 && t.unroll != 8)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: unroll must be 1, 2, 4 or 8");
+    if (t.ctas_per_sm < 1 || t.ctas_per_sm > 32)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ctas_per_sm outside [1, 32]");
+    return G2G_SUCCESS;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+} // namespace
+
+struct g2g_plan {
+    int device = 0;
+    int sm_count = 0;
+    int n_pairs = 0;
+    int n_ranks = 0;
+    std::vector<PairHost> host;
+    std::vector<g2g::PairInfo> pinfo;
+    std::vector<int32_t> splits;
+    std::vector<g2g::SrcEntry> src_tables;
+    std::vector<g2g::DstEntry> dst_tables;
+    int64_t n_parts = 0, n_cells = 0, max_cells_per_pair = 0;
+    int64_t bytes_moved = 0, bytes_min_traffic = 0;
+    bool any_trans = false;
+    int max_trans_esz = 0;
+    int paths = 0; // tile paths the work list needs (1 copy, 2 transpose, 4 scaled)
+    g2g_tuning tuning;
+    // device
+    void *dmem = nullptr;
+    size_t dmem_bytes = 0;
+    g2g::PlanDevice dev;
+    long long n_tiles = 0;
+    long long n_pieces = 0;
+    cudaStream_t last_stream = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t graph_stream = nullptr;
+};
+
+namespace {
+
+int64_t tile_capacity_bound(const PairHost &p, const g2g_tuning &t) {
+    const int64_t pr = p.a.nbr() + p.b.nbr() + 1, pc = p.a.nbc() + p.b.nbc() + 1;
+    int64_t bound = 0;
+    bool has_plain = false, has_trans = false;
+    for (const HBlock &b : p.a.blocks) {
+        if (b.trans) has_trans = true; else has_plain = true;
+    }
+    if (has_trans) {
+        const int64_t td = t.tile_dim;
+        bound += (p.m / td + pr) * (p.n / td + pc);
+    }
+    if (has_plain) {
+        const int64_t tile_rows = std::max<int64_t>(1, 4096 / p.esz);
+        const int64_t tcmin = std::max<int64_t>(1, t.tile_bytes / (tile_rows * p.esz));
+        bound += (p.m / tile_rows + pr) * (p.n / tcmin + pc);
+    }
+    return bound;
+}
+
+g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int dtype,
+                      const g2g_op *op, int pair_index, PairHost &p) {
+    (void)pair_index;
+    p.dtype = dtype;
+    p.esz = dtype_esz(dtype);
+    if (!p.esz)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "unknown dtype %d", dtype);
+    if (!di || !df)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "layout descriptor is NULL");
+    const int P = std::max(1, std::max(di->n_ranks, df->n_ranks));
+    G2G_TRY(load_layout(di, "initial", P, false, p.a));
+    G2G_TRY(load_layout(df, "final", P, true, p.b));
+    char trans = 'N';
+    if (op) {
+        trans = (char)std::toupper((unsigned char)op->trans);
+        if (trans != 'N' && trans != 'T' && trans != 'C')
+            return fail(G2G_ERROR_INVALID_ARGUMENT, "trans must be 'N', 'T' or 'C', got '%c'",
+                        op->trans);
+        p.alpha[0] = op->alpha[0];
+        p.alpha[1] = op->alpha[1];
+        p.beta[0] = op->beta[0];
+        p.beta[1] = op->beta[1];
+        if (!dtype_complex(dtype) && (p.alpha[1] != 0.0 || p.beta[1] != 0.0))
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "alpha/beta have an imaginary part but the dtype is real");
+    }
+    transpose_layout(p.a, trans);
+    if (p.a.rs.front() != p.b.rs.front() || p.a.rs.back() != p.b.rs.back() ||
+        p.a.cs.front() != p.b.cs.front() || p.a.cs.back() != p.b.cs.back())
+        return fail(G2G_ERROR_INVALID_ARGUMENT,
+                    "initial (after op '%c') and final layouts cover different matrices: "
+                    "rows [%d, %d) vs [%d, %d), cols [%d, %d) vs [%d, %d)",
+                    trans, p.a.rs.front(), p.a.rs.back(), p.b.rs.front(), p.b.rs.back(),
+                    p.a.cs.front(), p.a.cs.back(), p.b.cs.front(), p.b.cs.back());
+    // (alpha, beta) == (1, 0) in the element type is a plain copy
+    // (memory_utils.hpp:92-95, communication_data.cpp:165)
+    if (dtype == G2G_FLOAT32 || dtype == G2G_COMPLEX64) {
+        float ar = (float)p.alpha[0], ai = (float)p.alpha[1];
+        float br = (float)p.beta[0], bi = (float)p.beta[1];
+        p.scaled = !(ar == 1.0f && ai == 0.0f && br == 0.0f && bi == 0.0f);
+    } else {
+        p.scaled = !(p.alpha[0] == 1.0 && p.alpha[1] == 0.0 && p.beta[0] == 0.0 &&
+                     p.beta[1] == 0.0);
+    }
+    for (const HBlock &b : p.a.blocks)
+        if (b.trans)
+            p.any_trans = true;
+    p.m = p.b.rs.back() - p.b.rs.front();
+    p.n = p.b.cs.back() - p.b.cs.front();
+    return G2G_SUCCESS;
+}
+
+// Lays out the plan's host arrays and PairInfo offsets.
+void assemble(g2g_plan &pl) {
+    pl.pinfo.resize(pl.n_pairs);
+    pl.splits.clear();
+    pl.src_tables.clear();
+    pl.dst_tables.clear();
+    pl.n_parts = 0;
+    pl.n_cells = 0;
+    pl.max_cells_per_pair = 0;
+    pl.bytes_moved = 0;
+    pl.bytes_min_traffic = 0;
+    pl.any_trans = false;
+    pl.max_trans_esz = 0;
+    pl.paths = 0;
+    for (int k = 0; k < pl.n_pairs; ++k) {
+        PairHost &p = pl.host[k];
+        g2g::PairInfo &pi = pl.pinfo[k];
+        std::memset(&pi, 0, sizeof(pi));
+        pi.a_nr = p.a.nbr();
+        pi.a_nc = p.a.nbc();
+        pi.b_nr = p.b.nbr();
+        pi.b_nc = p.b.nbc();
+        pi.a_rs = (int32_t)pl.splits.size();
+        pl.splits.insert(pl.splits.end(), p.a.rs.begin(), p.a.rs.end());
+        pi.a_cs = (int32_t)pl.splits.size();
+        pl.splits.insert(pl.splits.end(), p.a.cs.begin(), p.a.cs.end());
+        pi.b_rs = (int32_t)pl.splits.size();
+        pl.splits.insert(pl.splits.end(), p.b.rs.begin(), p.b.rs.end());
+        pi.b_cs = (int32_t)pl.splits.size();
+        pl.splits.insert(pl.splits.end(), p.b.cs.begin(), p.b.cs.end());
+        pi.src_table = (int64_t)pl.src_tables.size();
+        pl.src_tables.resize(pl.src_tables.size() + (size_t)pi.a_nr * pi.a_nc);
+        for (const HBlock &b : p.a.blocks) {
+            g2g::SrcEntry &e = pl.src_tables[pi.src_table + (int64_t)b.row * pi.a_nc + b.col];
+            e.data = b.data;
+            e.ld = b.stride;
+            e.flags = (b.trans ? 1u : 0u) | (b.conj && dtype_complex(p.dtype) ? 2u : 0u);
+            e.pad = 0;
+        }
+        pi.dst_table = (int64_t)pl.dst_tables.size();
+        pl.dst_tables.resize(pl.dst_tables.size() + (size_t)pi.b_nr * pi.b_nc);
+        for (const HBlock &b : p.b.blocks) {
+            g2g::DstEntry &e = pl.dst_tables[pi.dst_table + (int64_t)b.row * pi.b_nc + b.col];
+            e.data = b.data;
+            e.ld = b.stride;
+        }
+        pi.row_parts = pl.n_parts;
+        pl.n_parts += pi.a_nr + pi.b_nr + 2;
+        pi.col_parts = pl.n_parts;
+        pl.n_parts += pi.a_nc + pi.b_nc + 2;
+        const int64_t cells = (int64_t)(pi.a_nr + pi.b_nr + 1) * (pi.a_nc + pi.b_nc + 1);
+        pi.cells = pl.n_cells;
+        pl.n_cells += cells;
+        pl.max_cells_per_pair = std::max(pl.max_cells_per_pair, cells);
+        pi.kind = esz_code(p.esz) | ((uint32_t)p.dtype << g2g::KIND_DTYPE_SHIFT) |
+                  (p.scaled ? g2g::KIND_SCALED : 0u);
+        pi.tile_rows = (int32_t)std::max(1, 4096 / p.esz);
+        pi.tile_bytes = pl.tuning.tile_bytes;
+        pi.tile_dim = pl.tuning.tile_dim;
+        pi.alpha[0] = p.alpha[0];
+        pi.alpha[1] = p.alpha[1];
+        pi.beta[0] = p.beta[0];
+        pi.beta[1] = p.beta[1];
+        const int64_t bytes = p.m * p.n * p.esz;
+        pl.bytes_moved += bytes;
+        pl.bytes_min_traffic += (p.scaled ? 3 : 2) * bytes;
+        if (p.any_trans) {
+            pl.any_trans = true;
+            pl.max_trans_esz = std::max(pl.max_trans_esz, p.esz);
+        }
+        bool any_plain = false;
+        for (const HBlock &b : p.a.blocks)
+            if (!b.trans)
+                any_plain = true;
+        if (p.scaled)
+            pl.paths |= 4;
+        else
+            pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0);
+    }
+}
+
+// Allocates device memory, uploads, runs the device planner, waits for it.
+g2g_status plan_on_device(g2g_plan &pl) {
+    DeviceState *ds = nullptr;
+    G2G_TRY(device_state(&ds, &pl.device));
+    pl.sm_count = ds->sm_count;
+    int64_t capacity = 0;
+    for (const PairHost &p : pl.host)
+        capacity += tile_capacity_bound(p, pl.tuning);
+    capacity = std::max<int64_t>(capacity, 1);
+
+    // sub-buffer layout of the single allocation
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align_up(off + std::max<size_t>(bytes, 1), 256);
+        return o;
+    };
+    const size_t o_pairs = take(sizeof(g2g::PairInfo) * pl.pinfo.size());
+    const size_t o_splits = take(sizeof(int32_t) * pl.splits.size());
+    const size_t o_src = take(sizeof(g2g::SrcEntry) * pl.src_tables.size());
+    const size_t o_dst = take(sizeof(g2g::DstEntry) * pl.dst_tables.size());
+    const size_t upload_end = off;
+    const size_t o_parts = take(sizeof(g2g::Part) * (size_t)pl.n_parts);
+    const size_t o_cells = take(sizeof(long long) * (size_t)pl.n_cells);
+    const size_t o_sums = take(sizeof(long long) * (size_t)g2g::scan_sums_capacity(pl.n_cells));
+    const size_t o_counters = take(64);
+    const size_t o_tiles = take(sizeof(g2g::Tile) * (size_t)capacity);
+    const size_t total = off;
+
+    if (pl.dmem && pl.dmem_bytes < total) {
+        G2G_CUDA(cudaStreamSynchronize(ds->plan_stream));
+        G2G_CUDA(cudaFreeAsync(pl.dmem, ds->plan_stream));
+        pl.dmem = nullptr;
+    }
+    if (!pl.dmem) {
+        G2G_CUDA(cudaMallocAsync(&pl.dmem, total, ds->plan_stream));
+        pl.dmem_bytes = total;
+    }
+    char *base = (char *)pl.dmem;
+    g2g::PlanDevice &d = pl.dev;
+    d.pairs = (g2g::PairInfo *)(base + o_pairs);
+    d.splits = (int32_t *)(base + o_splits);
+    d.src_tables = (g2g::SrcEntry *)(base + o_src);
+    d.dst_tables = (g2g::DstEntry *)(base + o_dst);
+    d.parts = (g2g::Part *)(base + o_parts);
+    d.cell_tiles = (long long *)(base + o_cells);
+    d.scan_sums = (long long *)(base + o_sums);
+    d.n_tiles = (long long *)(base + o_counters);
+    d.n_pieces = (unsigned long long *)(base + o_counters + 8);
+    d.overflow = (int *)(base + o_counters + 16);
+    d.tiles = (g2g::Tile *)(base + o_tiles);
+    d.tile_capacity = capacity;
+    d.max_cells_per_pair = pl.max_cells_per_pair;
+
+    // one pinned staging copy of everything the host built
+    std::vector<char> staging(upload_end, 0);
+    std::memcpy(staging.data() + o_pairs, pl.pinfo.data(),
+                sizeof(g2g::PairInfo) * pl.pinfo.size());
+    if (!pl.splits.empty())
+        std::memcpy(staging.data() + o_splits, pl.splits.data(),
+                    sizeof(int32_t) * pl.splits.size());
+    if (!pl.src_tables.empty())
+        std::memcpy(staging.data() + o_src, pl.src_tables.data(),
+                    sizeof(g2g::SrcEntry) * pl.src_tables.size());
+    if (!pl.dst_tables.empty())
+        std::memcpy(staging.data() + o_dst, pl.dst_tables.data(),
+                    sizeof(g2g::DstEntry) * pl.dst_tables.size());
+    std::lock_guard<std::mutex> lk(ds->mu);
+    if (ds->pinned_bytes < upload_end) {
+        if (ds->pinned)
+            cudaFreeHost(ds->pinned);
+        ds->pinned = nullptr;
+        ds->pinned_bytes = 0;
+        size_t want = std::max<size_t>(upload_end, (size_t)1 << 20);
+        G2G_CUDA(cudaMallocHost(&ds->pinned, want));
+        ds->pinned_bytes = want;
+    }
+    void *pinned = ds->pinned;
+    std::memcpy(pinned, staging.data(), upload_end);
+    cudaError_t e = cudaMemcpyAsync(base, pinned, upload_end, cudaMemcpyHostToDevice,
+                                    ds->plan_stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(base + o_counters, 0, 64, ds->plan_stream);
+    if (e == cudaSuccess)
+        e = g2g::launch_plan(d, pl.n_pairs, 0, pl.n_cells, ds->plan_stream);
+    long long counters[3] = {0, 0, 0};
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(pinned, base + o_counters, 24, cudaMemcpyDeviceToHost,
+                            ds->plan_stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ds->plan_stream);
+    if (e == cudaSuccess)
+        std::memcpy(counters, pinned, 24);
+    G2G_CUDA(e);
+    if (((int *)counters)[4] != 0)
+        return fail(G2G_ERROR_CUDA,
+                    "internal error: tile work list exceeded its bound (%lld > %lld)",
+                    counters[0], (long long)capacity);
+    pl.n_tiles = counters[0];
+    pl.n_pieces = counters[1];
+    return G2G_SUCCESS;
+}
+
+g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
+    g2g::ScatterConfig c;
+    c.threads = pl.tuning.threads;
+    c.unroll = pl.tuning.unroll;
+    c.ctas_per_sm = pl.tuning.ctas_per_sm;
+    c.tile_dim = pl.tuning.tile_dim;
+    long long g = (long long)pl.sm_count * pl.tuning.ctas_per_sm;
+    if (g > pl.n_tiles)
+        g = pl.n_tiles;
+    c.grid = (int)std::max<long long>(g, 1);
+    c.smem_bytes = pl.max_trans_esz ? g2g::transpose_smem_bytes(c.tile_dim, pl.max_trans_esz)
+                                    : 0;
+    c.paths = pl.paths ? pl.paths : 1;
+    return c;
+}
+
+g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layout_desc *finals,
+                       const g2g_dtype *dtypes, g2g_dtype single_dtype, const g2g_op *ops,
+                       g2g_plan **out) {
+    if (!out)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan output pointer is NULL");
+    *out = nullptr;
+    if (n_pairs < 1)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "n_pairs must be >= 1");
+    if (!inits || !finals)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "layout arrays are NULL");
+    g2g_plan *pl = new g2g_plan();
+    pl->n_pairs = n_pairs;
+    pl->tuning = default_tuning();
+    pl->host.resize(n_pairs);
+    for (int k = 0; k < n_pairs; ++k) {
+        int dt = dtypes ? (int)dtypes[k] : (int)single_dtype;
+        g2g_status st = build_pair(&inits[k], &finals[k], dt, ops ? &ops[k] : nullptr, k,
+                                   pl->host[k]);
+        if (st != G2G_SUCCESS) {
+            if (n_pairs > 1)
+                t_last_error = "pair " + std::to_string(k) + ": " + t_last_error;
+            delete pl;
+            return st;
+        }
+        pl->n_ranks = std::max(pl->n_ranks, std::max(inits[k].n_ranks, finals[k].n_ranks));
+    }
+    assemble(*pl);
+    g2g_status st = plan_on_device(*pl);
+    if (st != G2G_SUCCESS) {
+        g2g_plan_destroy(pl);
+        return st;
+    }
+    G2G_CUDA(cudaEventCreateWithFlags(&pl->done, cudaEventDisableTiming));
+    *out = pl;
+    return G2G_SUCCESS;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *g2g_last_error_string(void) { return t_last_error.c_str(); }
+
+const char *g2g_version_string(void) { return "grid2grid_gb300 0.1 (sm_103a)"; }
+
+g2g_status g2g_plan_create(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                           g2g_dtype dtype, const g2g_op *op, void *stream,
+                           g2g_plan **plan) {
+    (void)stream;
+    return create_plan(1, initial, final_, nullptr, dtype, op, plan);
+}
+
+g2g_status g2g_plan_create_batch(int32_t n_pairs, const g2g_layout_desc *initials,
+                                 const g2g_layout_desc *finals, const g2g_dtype *dtypes,
+                                 const g2g_op *ops, void *stream, g2g_plan **plan) {
+    (void)stream;
+    if (!dtypes)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "dtypes is NULL");
+    return create_plan(n_pairs, initials, finals, dtypes, G2G_FLOAT32, ops, plan);
+}
+
+g2g_status g2g_plan_execute(g2g_plan *plan, void *stream) {
+    if (!plan)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (plan->n_tiles > 0) {
+        if (plan->graph && plan->graph_stream == s) {
+            G2G_CUDA(cudaGraphLaunch(plan->graph, s));
+        } else {
+            G2G_CUDA(g2g::launch_scatter(plan->dev, scatter_config(*plan), s));
+        }
+    }
+    G2G_CUDA(cudaEventRecord(plan->done, s));
+    plan->last_stream = s;
+    return G2G_SUCCESS;
+}
+
+g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream) {
+    if (!plan)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!s)
+        return fail(G2G_ERROR_INVALID_ARGUMENT,
+                    "graph capture needs a non-default stream");
+    if (plan->graph) {
+        cudaGraphExecDestroy(plan->graph);
+        plan->graph = nullptr;
+    }
+    if (plan->n_tiles == 0)
+        return G2G_SUCCESS;
+    cudaGraph_t g = nullptr;
+    G2G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = g2g::launch_scatter(plan->dev, scatter_config(*plan), s);
+    cudaError_t ee = cudaStreamEndCapture(s, &g);
+    G2G_CUDA(le);
+    G2G_CUDA(ee);
+    cudaError_t ie = cudaGraphInstantiate(&plan->graph, g, 0);
+    cudaGraphDestroy(g);
+    G2G_CUDA(ie);
+    plan->graph_stream = s;
+    return G2G_SUCCESS;
+}
+
+g2g_status g2g_plan_set_tuning(g2g_plan *plan, const g2g_tuning *tuning) {
+    if (!plan || !tuning)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan or tuning is NULL");
+    g2g_tuning t = merge_tuning(plan->tuning, tuning);
+    G2G_TRY(check_tuning(t));
+    const bool replan = t.tile_bytes != plan->tuning.tile_bytes ||
+                        t.tile_dim != plan->tuning.tile_dim;
+    plan->tuning = t;
+    if (plan->graph) {
+        cudaGraphExecDestroy(plan->graph);
+        plan->graph = nullptr;
+    }
+    if (replan) {
+        // the work list may be in use by queued executions
+        if (plan->last_stream || plan->done)
+            G2G_CUDA(cudaEventSynchronize(plan->done));
+        assemble(*plan);
+        G2G_TRY(plan_on_device(*plan));
+    }
+    return G2G_SUCCESS;
+}
+
+g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tuning *best) {
+    if (!plan)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan is NULL");
+    if (iters < 1)
+        iters = 3;
+    cudaStream_t s = (cudaStream_t)stream;
+    const g2g_tuning start = plan->tuning;
+    std::vector<g2g_tuning> cands;
+    const int tile_bytes_opts[] = {16 * 1024, 32 * 1024, 64 * 1024};
+    const int tile_dim_opts[] = {32, 64};
+    const int threads_opts[] = {256, 512};
+    const int unroll_opts[] = {2, 4, 8};
+    const int ctas_opts[] = {2, 4, 8};
+    for (int tb : tile_bytes_opts)
+        for (int td : tile_dim_opts) {
+            if (!plan->any_trans && td != start.tile_dim)
+                continue;
+            for (int th : threads_opts)
+                for (int u : unroll_opts)
+                    for (int c : ctas_opts) {
+                        if (th * c > 2048)
+                            continue;
+                        g2g_tuning t = start;
+                        t.tile_bytes = tb;
+                        t.tile_dim = td;
+                        t.threads = th;
+                        t.unroll = u;
+                        t.ctas_per_sm = c;
+                        cands.push_back(t);
+                    }
+        }
+    cudaEvent_t e0, e1;
+    G2G_CUDA(cudaEventCreate(&e0));
+    G2G_CUDA(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    g2g_tuning best_t = start;
+    for (const g2g_tuning &t : cands) {
+        g2g_status st = g2g_plan_set_tuning(plan, &t);
+        if (st != G2G_SUCCESS)
+            continue;
+        if (g2g_plan_execute(plan, s) != G2G_SUCCESS) // warm-up
+            continue;
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < iters; ++i)
+            g2g_plan_execute(plan, s);
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess)
+            break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_t = plan->tuning;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    G2G_TRY(g2g_plan_set_tuning(plan, &best_t));
+    if (best)
+        *best = plan->tuning;
+    return G2G_SUCCESS;
+}
+
+g2g_status g2g_plan_get_info(const g2g_plan *plan, g2g_plan_info *info) {
+    if (!plan || !info)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan or info is NULL");
+    std::memset(info, 0, sizeof(*info));
+    info->n_pairs = plan->n_pairs;
+    info->n_ranks = plan->n_ranks;
+    info->n_pieces = plan->n_pieces;
+    info->n_tiles = plan->n_tiles;
+    info->bytes_moved = plan->bytes_moved;
+    info->bytes_min_traffic = plan->bytes_min_traffic;
+    info->metadata_bytes = (int64_t)plan->dmem_bytes;
+    info->graph_captured = plan->graph ? 1 : 0;
+    info->tuning = plan->tuning;
+    return G2G_SUCCESS;
+}
+
+g2g_status g2g_plan_destroy(g2g_plan *plan) {
+    if (!plan)
+        return G2G_SUCCESS;
+    g2g_status st = G2G_SUCCESS;
+    if (plan->graph)
+        cudaGraphExecDestroy(plan->graph);
+    if (plan->dmem) {
+        DeviceState *ds = nullptr;
+        if (device_state(&ds, nullptr) == G2G_SUCCESS) {
+            // free after the last execution that used the plan
+            if (plan->done && plan->last_stream != nullptr)
+                cudaStreamWaitEvent(ds->plan_stream, plan->done, 0);
+            else if (plan->done)
+                cudaEventSynchronize(plan->done);
+            cudaError_t e = cudaFreeAsync(plan->dmem, ds->plan_stream);
+            if (e != cudaSuccess)
+                st = fail(G2G_ERROR_CUDA, "cudaFreeAsync failed: %s", cudaGetErrorString(e));
+        }
+    }
+    if (plan->done)
+        cudaEventDestroy(plan->done);
+    delete plan;
+    return st;
+}
+
+g2g_status g2g_transform(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                         g2g_dtype dtype, const g2g_op *op, void *stream) {
+    g2g_plan *plan = nullptr;
+    G2G_TRY(g2g_plan_create(initial, final_, dtype, op, stream, &plan));
+    g2g_status st = g2g_plan_execute(plan, stream);
+    if (st == G2G_SUCCESS) {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess)
+            st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
+    }
+    g2g_status st2 = g2g_plan_destroy(plan);
+    return st != G2G_SUCCESS ? st : st2;
+}
+
+g2g_status g2g_transform_batch(int32_t n_pairs, const g2g_layout_desc *initials,
+                               const g2g_layout_desc *finals, const g2g_dtype *dtypes,
+                               const g2g_op *ops, void *stream) {
+    g2g_plan *plan = nullptr;
+    G2G_TRY(g2g_plan_create_batch(n_pairs, initials, finals, dtypes, ops, stream, &plan));
+    g2g_status st = g2g_plan_execute(plan, stream);
+    if (st == G2G_SUCCESS) {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess)
+            st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
+    }
+    g2g_status st2 = g2g_plan_destroy(plan);
+    return st != G2G_SUCCESS ? st : st2;
+}
+
+g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a, const int32_t *splits_b,
+                          int32_t n_b, int32_t *start_index, int32_t *end_index,
+                          void *stream) {
+    if (!splits_a || !splits_b || n_a < 1 || n_b < 1 || (n_a > 1 && (!start_index || !end_index)))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "grid cover: bad arguments");
+    G2G_TRY(check_splits(splits_a, n_a - 1, "first", "cover"));
+    G2G_TRY(check_splits(splits_b, n_b - 1, "second", "cover"));
+    if (splits_a[0] != splits_b[0] || splits_a[n_a - 1] != splits_b[n_b - 1])
+        return fail(G2G_ERROR_INVALID_ARGUMENT,
+                    "grid cover: split vectors must share their first and last entries");
+    if (n_a == 1)
+        return G2G_SUCCESS;
+    cudaStream_t s = (cudaStream_t)stream;
+    int32_t *d = nullptr;
+    const size_t bytes = sizeof(int32_t) * ((size_t)n_a + n_b + 2 * (size_t)(n_a - 1));
+    G2G_CUDA(cudaMallocAsync((void **)&d, bytes, s));
+    int32_t *da = d, *db = d + n_a, *ds = db + n_b, *de = ds + (n_a - 1);
+    cudaError_t e = cudaMemcpyAsync(da, splits_a, sizeof(int32_t) * n_a,
+                                    cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(db, splits_b, sizeof(int32_t) * n_b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = g2g::launch_cover(da, n_a, db, n_b, ds, de, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(start_index, ds, sizeof(int32_t) * (n_a - 1),
+                            cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(end_index, de, sizeof(int32_t) * (n_a - 1),
+                            cudaMemcpyDeviceToHost, s);
+    cudaError_t fe = cudaFreeAsync(d, s);
+    if (e == cudaSuccess)
+        e = fe;
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    G2G_CUDA(e);
+    return G2G_SUCCESS;
+}
+
+} // extern "C"

@@ -1,0 +1,54 @@
+// Host-callable launchers for the device code (planner and gather-scatter).
+#pragma once
+
+#include "g2g_internal.hpp"
+
+#include <cuda_runtime.h>
+
+namespace g2g {
+
+// Device pointers of one plan's metadata (all inside one allocation).
+struct PlanDevice {
+    PairInfo *pairs = nullptr;
+    int32_t *splits = nullptr;
+    SrcEntry *src_tables = nullptr;
+    DstEntry *dst_tables = nullptr;
+    Part *parts = nullptr;
+    long long *cell_tiles = nullptr;   // counts, then exclusive offsets
+    long long *scan_sums = nullptr;
+    Tile *tiles = nullptr;
+    long long *n_tiles = nullptr;      // device scalar: tiles in the work list
+    unsigned long long *n_pieces = nullptr;
+    int *overflow = nullptr;           // device flag: tile capacity exceeded
+    long long tile_capacity = 0;
+    long long max_cells_per_pair = 0;
+};
+
+// Runs the device planner (merge, tile counts, scan, emission) on `stream`.
+cudaError_t launch_plan(const PlanDevice &d, int n_pairs, int unused,
+                        long long n_cells, cudaStream_t stream);
+long long scan_sums_capacity(long long n_cells);
+
+// Grid cover (interval_cover form) of split vector a by b, device arrays.
+cudaError_t launch_cover(const int32_t *a, int na, const int32_t *b, int nb,
+                         int32_t *start, int32_t *end, cudaStream_t stream);
+
+struct ScatterConfig {
+    int threads = 256;       // 128, 256 or 512
+    int unroll = 4;          // 1, 2, 4 or 8
+    int grid = 0;            // CTAs (persistent); 0 = SM count x ctas_per_sm
+    int ctas_per_sm = 4;
+    int tile_dim = 32;       // transposed tile edge (16, 32 or 64)
+    size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
+    int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled
+};
+
+// Shared memory a transposed tile of edge `tile_dim` with elements of `esz`
+// bytes needs.
+size_t transpose_smem_bytes(int tile_dim, int esz);
+
+// Launches the gather-scatter over d.tiles[0, *d.n_tiles).
+cudaError_t launch_scatter(const PlanDevice &d, const ScatterConfig &cfg,
+                           cudaStream_t stream);
+
+} // namespace g2g

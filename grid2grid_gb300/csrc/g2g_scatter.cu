@@ -1,0 +1,545 @@
+// The gather-scatter: one persistent kernel that replaces the reference's
+// pack (communication_data.cpp:132-142), MPI exchange (transform.cpp:41-124),
+// local copy (communication_data.cpp:224-252) and unpack
+// (communication_data.cpp:157-173). Every tile of the work list is a
+// sub-rectangle of one piece (initial block x final block); its source is read
+// once and its destination written once, straight from the initial owner's
+// strided block into the final owner's strided block.
+//
+// Three tile paths (uniform per tile, so no divergence):
+//  * copy_tile       plain, non-transposed: byte movement in 16-byte chunks
+//                    aligned to the DESTINATION. When source and destination
+//                    are misaligned differently (arbitrary strides), the
+//                    source window is assembled from this lane's 16-byte load
+//                    and the next lane's (warp shuffle), then funnel-shifted
+//                    by whole words. Loads and stores are 128-bit; only the
+//                    head and tail chunk of a column store single words.
+//                    (memory_utils.hpp:41-77)
+//  * transpose_tile  plain, transposed (+ conjugated): a tile staged through
+//                    shared memory with a padded pitch, loaded coalesced along
+//                    the source's storage columns and stored coalesced along
+//                    the destination's columns (memory_utils.hpp:124-184).
+//  * scaled tiles    dst = beta*dst + alpha*op(src) in the element type with
+//                    the rounding of the reference's host arithmetic: every
+//                    product and sum rounded separately, complex products in
+//                    the C99 Annex G form that GCC's std::complex multiply uses
+//                    (memory_utils.hpp:25-39,79-122,186-256).
+#include "g2g_internal.hpp"
+#include "g2g_launch.hpp"
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace g2g {
+
+namespace {
+
+// ---------------------------------------------------------------- memory ops
+__device__ __forceinline__ uint4 ldg_v4(uint64_t addr) {
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(addr));
+    return v;
+}
+
+__device__ __forceinline__ void st_v4(uint64_t addr, uint4 v) {
+    asm volatile("st.global.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(addr), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ void st_u32(uint64_t addr, uint32_t v) {
+    asm volatile("st.global.u32 [%0], %1;" ::"l"(addr), "r"(v) : "memory");
+}
+
+template <typename W> __device__ __forceinline__ W ldg_w(uint64_t addr);
+template <> __device__ __forceinline__ uint32_t ldg_w<uint32_t>(uint64_t a) {
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(a));
+    return v;
+}
+template <> __device__ __forceinline__ unsigned long long ldg_w<unsigned long long>(uint64_t a) {
+    unsigned long long v;
+    asm("ld.global.nc.L1::no_allocate.u64 %0, [%1];" : "=l"(v) : "l"(a));
+    return v;
+}
+template <> __device__ __forceinline__ uint4 ldg_w<uint4>(uint64_t a) { return ldg_v4(a); }
+
+template <typename W> __device__ __forceinline__ void st_w(uint64_t addr, W v);
+template <> __device__ __forceinline__ void st_w<uint32_t>(uint64_t a, uint32_t v) {
+    st_u32(a, v);
+}
+template <> __device__ __forceinline__ void st_w<unsigned long long>(uint64_t a,
+                                                                     unsigned long long v) {
+    asm volatile("st.global.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+template <> __device__ __forceinline__ void st_w<uint4>(uint64_t a, uint4 v) { st_v4(a, v); }
+
+// Flip the sign bit of the highest 32-bit word of an element: the sign of the
+// imaginary part of a little-endian std::complex<float|double>, i.e.
+// std::conj (block.cpp:15-21), NaN payloads included.
+__device__ __forceinline__ void flip_top_sign(uint32_t &w) { w ^= 0x80000000u; }
+__device__ __forceinline__ void flip_top_sign(unsigned long long &w) {
+    w ^= 0x8000000000000000ull;
+}
+__device__ __forceinline__ void flip_top_sign(uint4 &w) { w.w ^= 0x80000000u; }
+
+// word-granular funnel: 4 words starting at word q of the 8-word window lo:hi
+__device__ __forceinline__ uint4 funnel_words(uint4 lo, uint4 hi, uint32_t q) {
+    uint32_t a0, a1, a2, a3, a4;
+    if (q & 2u) {
+        a0 = lo.z; a1 = lo.w; a2 = hi.x; a3 = hi.y; a4 = hi.z;
+    } else {
+        a0 = lo.x; a1 = lo.y; a2 = lo.z; a3 = lo.w; a4 = hi.x;
+    }
+    uint4 o;
+    if (q & 1u) {
+        o.x = a1; o.y = a2; o.z = a3; o.w = a4;
+    } else {
+        o.x = a0; o.y = a1; o.z = a2; o.w = a3;
+    }
+    return o;
+}
+
+// ------------------------------------------------------------ plain copy tile
+template <int THREADS, int U>
+__device__ __forceinline__ void copy_tile(const Tile &t) {
+    constexpr int NWARP = THREADS / 32;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int esz = kind_esz(t.kind);
+    const long long L = (long long)t.rows * esz; // bytes per column
+    if (L <= 0 || t.cols <= 0)
+        return;
+    // destination-aligned 16-byte chunks a column can touch
+    const int cpc = (int)((L + 27) >> 4);
+    int lpc_shift = 0;
+    while ((1 << lpc_shift) < cpc && lpc_shift < 5)
+        ++lpc_shift;
+    const int lpc = 1 << lpc_shift;          // lanes per column
+    const int cpw = 32 >> lpc_shift;         // columns per warp step
+    const int sub = lane >> lpc_shift;
+    const int kl = lane & (lpc - 1);
+    const bool last_in_group = kl == lpc - 1;
+    const int col_step = NWARP * cpw;
+    const int warp_col0 = warp * cpw;
+    const int ncolit =
+        t.cols > warp_col0 ? (t.cols - warp_col0 + col_step - 1) / col_step : 0;
+    const int nkit = (cpc + lpc - 1) >> lpc_shift;
+    const int my_col0 = warp_col0 + sub;
+
+    int colit = 0, kit = 0;
+    while (colit < ncolit) { // warp-uniform
+        uint4 lo[U], hx[U];
+        uint64_t chunk[U];
+        uint32_t q[U], wm[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = my_col0 + colit * col_step;
+            const bool colok = (colit < ncolit) && (c < t.cols);
+            const uint64_t d = t.dst + (uint64_t)((long long)c * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+            const uint64_t ch = (d & ~15ull) + ((uint64_t)(kl + (kit << lpc_shift)) << 4);
+            const uint64_t vlo = ch > d ? ch : d;
+            const uint64_t dend = d + (uint64_t)L;
+            const uint64_t vhi = (ch + 16 < dend) ? ch + 16 : dend;
+            uint32_t m = 0;
+            if (colok && vlo < vhi) {
+                const uint32_t w0 = (uint32_t)(vlo - ch) >> 2;
+                const uint32_t w1 = (uint32_t)(vhi - ch) >> 2;
+                m = ((1u << w1) - 1u) & ~((1u << w0) - 1u);
+            }
+            const uint64_t win = ch + (s - d); // source address of the chunk's first byte
+            const uint32_t shb = (uint32_t)(win & 15u);
+            const uint64_t la = win - shb;
+            const uint64_t send = s + (uint64_t)L;
+            // load only 16-byte blocks that overlap the source column, so no
+            // access leaves the pages the column lives in
+            const bool need_lo = colok && (la < send) && (la + 16 > s);
+            lo[u] = need_lo ? ldg_v4(la) : make_uint4(0u, 0u, 0u, 0u);
+            const bool need_hi =
+                colok && last_in_group && shb != 0 && (la + 16 < send) && (la + 32 > s);
+            hx[u] = need_hi ? ldg_v4(la + 16) : make_uint4(0u, 0u, 0u, 0u);
+            chunk[u] = ch;
+            q[u] = shb >> 2;
+            wm[u] = m;
+            if (++kit == nkit) {
+                kit = 0;
+                ++colit;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            uint4 nb;
+            nb.x = __shfl_down_sync(0xffffffffu, lo[u].x, 1);
+            nb.y = __shfl_down_sync(0xffffffffu, lo[u].y, 1);
+            nb.z = __shfl_down_sync(0xffffffffu, lo[u].z, 1);
+            nb.w = __shfl_down_sync(0xffffffffu, lo[u].w, 1);
+            const uint4 hi = last_in_group ? hx[u] : nb;
+            const uint4 o = q[u] ? funnel_words(lo[u], hi, q[u]) : lo[u];
+            const uint32_t m = wm[u];
+            if (m == 0xFu) {
+                st_v4(chunk[u], o);
+            } else if (m) {
+                if (m & 1u) st_u32(chunk[u], o.x);
+                if (m & 2u) st_u32(chunk[u] + 4, o.y);
+                if (m & 4u) st_u32(chunk[u] + 8, o.z);
+                if (m & 8u) st_u32(chunk[u] + 12, o.w);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------ plain transposed tile
+template <typename W, int NWE> struct ElemW {
+    W w[NWE];
+};
+
+template <int THREADS, typename W, int NWE>
+__device__ __forceinline__ void transpose_tile(const Tile &t, unsigned char *smem_raw,
+                                               int td, bool conj) {
+    constexpr int NWARP = THREADS / 32;
+    constexpr int E = (int)sizeof(W) * NWE;
+    typedef ElemW<W, NWE> El;
+    El *smem = reinterpret_cast<El *>(smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int R = t.rows, C = t.cols;
+    const int pitch = td + 1;
+    // load: storage column r (final row r) holds C contiguous elements
+    for (int c0 = 0; c0 < C; c0 += 32) {
+        const int c = c0 + lane;
+        for (int rb = warp; rb < R; rb += 4 * NWARP) {
+            El v[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = rb + i * NWARP;
+                if (r < R && c < C) {
+                    const uint64_t p = t.src + (uint64_t)((long long)r * t.src_ld +
+                                                          (long long)c * E);
+#pragma unroll
+                    for (int k = 0; k < NWE; ++k)
+                        v[i].w[k] = ldg_w<W>(p + (uint64_t)k * sizeof(W));
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = rb + i * NWARP;
+                if (r < R && c < C)
+                    smem[r * pitch + c] = v[i];
+            }
+        }
+    }
+    __syncthreads();
+    // store: destination column c, lanes along its rows
+    for (int r0 = 0; r0 < R; r0 += 32) {
+        const int r = r0 + lane;
+        if (r < R) {
+            for (int c = warp; c < C; c += NWARP) {
+                El e = smem[r * pitch + c];
+                if (conj)
+                    flip_top_sign(e.w[NWE - 1]);
+                const uint64_t p = t.dst + (uint64_t)((long long)c * t.dst_ld +
+                                                      (long long)r * E);
+#pragma unroll
+                for (int k = 0; k < NWE; ++k)
+                    st_w<W>(p + (uint64_t)k * sizeof(W), e.w[k]);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// --------------------------------------------------------------- scaled tiles
+struct cplxf {
+    float x, y;
+};
+struct cplxd {
+    double x, y;
+};
+
+template <typename T> __device__ __forceinline__ T ld_elem(uint64_t a);
+template <> __device__ __forceinline__ float ld_elem<float>(uint64_t a) {
+    return *reinterpret_cast<const float *>(a);
+}
+template <> __device__ __forceinline__ double ld_elem<double>(uint64_t a) {
+    return *reinterpret_cast<const double *>(a);
+}
+template <> __device__ __forceinline__ cplxf ld_elem<cplxf>(uint64_t a) {
+    const float *p = reinterpret_cast<const float *>(a);
+    return cplxf{p[0], p[1]};
+}
+template <> __device__ __forceinline__ cplxd ld_elem<cplxd>(uint64_t a) {
+    const double *p = reinterpret_cast<const double *>(a);
+    return cplxd{p[0], p[1]};
+}
+template <typename T> __device__ __forceinline__ void st_elem(uint64_t a, T v);
+template <> __device__ __forceinline__ void st_elem<float>(uint64_t a, float v) {
+    *reinterpret_cast<float *>(a) = v;
+}
+template <> __device__ __forceinline__ void st_elem<double>(uint64_t a, double v) {
+    *reinterpret_cast<double *>(a) = v;
+}
+template <> __device__ __forceinline__ void st_elem<cplxf>(uint64_t a, cplxf v) {
+    float *p = reinterpret_cast<float *>(a);
+    p[0] = v.x;
+    p[1] = v.y;
+}
+template <> __device__ __forceinline__ void st_elem<cplxd>(uint64_t a, cplxd v) {
+    double *p = reinterpret_cast<double *>(a);
+    p[0] = v.x;
+    p[1] = v.y;
+}
+
+__device__ __forceinline__ float conj_elem(float v) { return v; }
+__device__ __forceinline__ double conj_elem(double v) { return v; }
+__device__ __forceinline__ cplxf conj_elem(cplxf v) {
+    v.y = __int_as_float(__float_as_int(v.y) ^ 0x80000000);
+    return v;
+}
+__device__ __forceinline__ cplxd conj_elem(cplxd v) {
+    v.y = __longlong_as_double(__double_as_longlong(v.y) ^ (long long)0x8000000000000000ull);
+    return v;
+}
+
+// Rounded-separately arithmetic (no contraction into FMA).
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+
+// Complex product as GCC computes std::complex<R> * std::complex<R>: the
+// textbook formula with each operation rounded, and when both parts come out
+// NaN the recovery of C99 Annex G (G.5.1, multiplicative operators): boxed
+// infinities, NaN operands set to signed zeros, recomputation scaled by inf.
+template <typename R>
+__device__ __forceinline__ void cmul(R a, R b, R c, R d, R &x, R &y) {
+    const R ac = rmul(a, c), bd = rmul(b, d), ad = rmul(a, d), bc = rmul(b, c);
+    x = rsub(ac, bd);
+    y = radd(ad, bc);
+    if (isnan(x) && isnan(y)) {
+        bool recalc = false;
+        const R one = R(1), zero = R(0);
+        if (isinf(a) || isinf(b)) {
+            a = copysign(isinf(a) ? one : zero, a);
+            b = copysign(isinf(b) ? one : zero, b);
+            if (isnan(c)) c = copysign(zero, c);
+            if (isnan(d)) d = copysign(zero, d);
+            recalc = true;
+        }
+        if (isinf(c) || isinf(d)) {
+            c = copysign(isinf(c) ? one : zero, c);
+            d = copysign(isinf(d) ? one : zero, d);
+            if (isnan(a)) a = copysign(zero, a);
+            if (isnan(b)) b = copysign(zero, b);
+            recalc = true;
+        }
+        if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
+            if (isnan(a)) a = copysign(zero, a);
+            if (isnan(b)) b = copysign(zero, b);
+            if (isnan(c)) c = copysign(zero, c);
+            if (isnan(d)) d = copysign(zero, d);
+            recalc = true;
+        }
+        if (recalc) {
+            const R inf = R(INFINITY);
+            x = rmul(inf, rsub(rmul(a, c), rmul(b, d)));
+            y = rmul(inf, radd(rmul(a, d), rmul(b, c)));
+        }
+    }
+}
+
+// beta*d + alpha*v, as memory_utils.hpp:36 / :111 / :236 evaluate it.
+__device__ __forceinline__ float axpby(float alpha, float v, float beta, float d) {
+    return radd(rmul(beta, d), rmul(alpha, v));
+}
+__device__ __forceinline__ double axpby(double alpha, double v, double beta, double d) {
+    return radd(rmul(beta, d), rmul(alpha, v));
+}
+__device__ __forceinline__ cplxf axpby(cplxf alpha, cplxf v, cplxf beta, cplxf d) {
+    float bx, by, ax, ay;
+    cmul(beta.x, beta.y, d.x, d.y, bx, by);
+    cmul(alpha.x, alpha.y, v.x, v.y, ax, ay);
+    return cplxf{radd(bx, ax), radd(by, ay)};
+}
+__device__ __forceinline__ cplxd axpby(cplxd alpha, cplxd v, cplxd beta, cplxd d) {
+    double bx, by, ax, ay;
+    cmul(beta.x, beta.y, d.x, d.y, bx, by);
+    cmul(alpha.x, alpha.y, v.x, v.y, ax, ay);
+    return cplxd{radd(bx, ax), radd(by, ay)};
+}
+
+template <typename T> __device__ __forceinline__ T scalar_from(const double *v);
+template <> __device__ __forceinline__ float scalar_from<float>(const double *v) {
+    return (float)v[0];
+}
+template <> __device__ __forceinline__ double scalar_from<double>(const double *v) {
+    return v[0];
+}
+template <> __device__ __forceinline__ cplxf scalar_from<cplxf>(const double *v) {
+    return cplxf{(float)v[0], (float)v[1]};
+}
+template <> __device__ __forceinline__ cplxd scalar_from<cplxd>(const double *v) {
+    return cplxd{v[0], v[1]};
+}
+
+template <int THREADS, typename T>
+__device__ __forceinline__ void scaled_tile(const Tile &t, const PairInfo *pairs,
+                                            unsigned char *smem_raw, int td) {
+    constexpr int NWARP = THREADS / 32;
+    constexpr int E = (int)sizeof(T);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T alpha = scalar_from<T>(pairs[t.pair].alpha);
+    const T beta = scalar_from<T>(pairs[t.pair].beta);
+    const int R = t.rows, C = t.cols;
+    if (!(t.kind & KIND_TRANS)) {
+        for (int c = warp; c < C; c += NWARP) {
+            const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
+            const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+            for (int r = lane; r < R; r += 32) {
+                const T v = ld_elem<T>(sc + (uint64_t)r * E);
+                const T d = ld_elem<T>(dc + (uint64_t)r * E);
+                st_elem<T>(dc + (uint64_t)r * E, axpby(alpha, v, beta, d));
+            }
+        }
+        return;
+    }
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    T *smem = reinterpret_cast<T *>(smem_raw);
+    const int pitch = td + 1;
+    for (int r = warp; r < R; r += NWARP)
+        for (int c = lane; c < C; c += 32)
+            smem[r * pitch + c] =
+                ld_elem<T>(t.src + (uint64_t)((long long)r * t.src_ld + (long long)c * E));
+    __syncthreads();
+    for (int c = warp; c < C; c += NWARP) {
+        const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+        for (int r = lane; r < R; r += 32) {
+            T v = smem[r * pitch + c];
+            if (conj)
+                v = conj_elem(v);
+            const T d = ld_elem<T>(dc + (uint64_t)r * E);
+            st_elem<T>(dc + (uint64_t)r * E, axpby(alpha, v, beta, d));
+        }
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------ kernel
+template <int THREADS>
+__device__ __forceinline__ void transpose_dispatch(const Tile &t, unsigned char *smem,
+                                                   int td) {
+    const int esz = kind_esz(t.kind);
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    const uint64_t a = t.src | t.dst | (uint64_t)t.src_ld | (uint64_t)t.dst_ld;
+    if (esz == 4) {
+        transpose_tile<THREADS, uint32_t, 1>(t, smem, td, conj);
+    } else if (esz == 8) {
+        if ((a & 7u) == 0)
+            transpose_tile<THREADS, unsigned long long, 1>(t, smem, td, conj);
+        else
+            transpose_tile<THREADS, uint32_t, 2>(t, smem, td, conj);
+    } else {
+        if ((a & 15u) == 0)
+            transpose_tile<THREADS, uint4, 1>(t, smem, td, conj);
+        else if ((a & 7u) == 0)
+            transpose_tile<THREADS, unsigned long long, 2>(t, smem, td, conj);
+        else
+            transpose_tile<THREADS, uint32_t, 4>(t, smem, td, conj);
+    }
+}
+
+template <int THREADS>
+__device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *pairs,
+                                                unsigned char *smem, int td) {
+    switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0: scaled_tile<THREADS, float>(t, pairs, smem, td); break;
+    case 1: scaled_tile<THREADS, double>(t, pairs, smem, td); break;
+    case 2: scaled_tile<THREADS, cplxf>(t, pairs, smem, td); break;
+    default: scaled_tile<THREADS, cplxd>(t, pairs, smem, td); break;
+    }
+}
+
+// Tile paths a kernel instance contains; a plan launches the smallest
+// instance that covers its tiles, so the plain copy does not carry the
+// register cost of the scaled complex arithmetic.
+enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
+
+// At least 1024 resident threads per SM (64 registers a thread): with U
+// 16-byte loads in flight per thread that keeps >= 32 KB of reads in flight
+// per SM, what HBM3e needs at this SM count.
+template <int THREADS, int U, int PATHS>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS)
+    scatter_kernel(const Tile *__restrict__ tiles, const long long *__restrict__ n_tiles_p,
+                   long long capacity, const PairInfo *__restrict__ pairs, int td) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    long long n = *n_tiles_p;
+    if (n > capacity)
+        n = capacity;
+    for (long long ti = blockIdx.x; ti < n; ti += gridDim.x) {
+        const Tile t = tiles[ti];
+        const uint32_t k = t.kind;
+        if ((PATHS & PATH_COPY) && !(k & (KIND_TRANS | KIND_SCALED)))
+            copy_tile<THREADS, U>(t);
+        else if ((PATHS & PATH_TRANSPOSE) && (k & KIND_TRANS) && !(k & KIND_SCALED))
+            transpose_dispatch<THREADS>(t, smem, td);
+        else if (PATHS & PATH_SCALED)
+            scaled_dispatch<THREADS>(t, pairs, smem, td);
+    }
+}
+
+template <int THREADS, int U, int PATHS>
+cudaError_t launch_t(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+    auto k = scatter_kernel<THREADS, U, PATHS>;
+    if (cfg.smem_bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)cfg.smem_bytes);
+        if (e != cudaSuccess)
+            return e;
+    }
+    k<<<cfg.grid, THREADS, cfg.smem_bytes, s>>>(d.tiles, d.n_tiles, d.tile_capacity, d.pairs,
+                                                cfg.tile_dim);
+    return cudaGetLastError();
+}
+
+template <int THREADS, int PATHS>
+cudaError_t launch_u(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+    switch (cfg.unroll) {
+    case 1: return launch_t<THREADS, 1, PATHS>(d, cfg, s);
+    case 2: return launch_t<THREADS, 2, PATHS>(d, cfg, s);
+    case 8: return launch_t<THREADS, 8, PATHS>(d, cfg, s);
+    default: return launch_t<THREADS, 4, PATHS>(d, cfg, s);
+    }
+}
+
+template <int THREADS>
+cudaError_t launch_p(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+    if (cfg.paths & PATH_SCALED)
+        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(d, cfg, s);
+    if (cfg.paths == PATH_COPY)
+        return launch_u<THREADS, PATH_COPY>(d, cfg, s);
+    if (cfg.paths == PATH_TRANSPOSE)
+        return launch_u<THREADS, PATH_TRANSPOSE>(d, cfg, s);
+    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(d, cfg, s);
+}
+
+} // namespace
+
+size_t transpose_smem_bytes(int tile_dim, int esz) {
+    return (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;
+}
+
+cudaError_t launch_scatter(const PlanDevice &d, const ScatterConfig &cfg,
+                           cudaStream_t stream) {
+    if (cfg.grid <= 0)
+        return cudaErrorInvalidConfiguration;
+    switch (cfg.threads) {
+    case 128: return launch_p<128>(d, cfg, stream);
+    case 512: return launch_p<512>(d, cfg, stream);
+    default: return launch_p<256>(d, cfg, stream);
+    }
+}
+
+} // namespace g2g

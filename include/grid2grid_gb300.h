@@ -1,0 +1,224 @@
+/*
+ * grid2grid_gb300 -- C ABI of the GB300-native grid2grid transform path.
+ *
+ * A matrix is split into a grid of blocks (grid2D: rows_split, cols_split);
+ * every block is owned by one rank (assigned_grid2D: ranks[i][j]) and stored
+ * column-major at an arbitrary pointer with an arbitrary stride (block<T>).
+ * A transform redistributes the matrix from an initial layout into a final
+ * layout:  final = beta * final + alpha * op(initial),  op in {N, T, C}.
+ *
+ * On one GPU the P ranks of a layout are *virtual ranks*: every rank's local
+ * blocks live in the same device memory, so a layout descriptor carries the
+ * local blocks of all ranks at once, each tagged with its rank. The
+ * reference's pack / MPI exchange / unpack collapses into one device
+ * gather-scatter over a work list that the device builds from the grid cover.
+ *
+ * Conventions
+ *  - Every function returns a g2g_status; on failure a human-readable message
+ *    is available from g2g_last_error_string() (thread-local).
+ *  - Pointers in g2g_block_desc.data are DEVICE addresses owned by the caller.
+ *    The library never frees them and never touches a destination block's
+ *    padding (rows < stride).
+ *  - A `stream` argument is a cudaStream_t passed as void* (NULL = legacy
+ *    default stream). All device work is stream-ordered.
+ *  - No function takes or returns a framework (torch/numpy) type.
+ *
+ * Reference interfaces replaced (paths inside kabicm/grid2grid):
+ *  - grid2grid::transform, 4 overloads           src/grid2grid/transform.hpp:13-43
+ *  - grid2grid::transformer<T>                    src/grid2grid/transformer.hpp:8-62
+ *  - grid2grid::grid_cover / get_decomp_cover     src/grid2grid/grid_cover.hpp:38-65,
+ *                                                 src/grid2grid/grid_cover.cpp:54-121
+ *  - grid_layout / assigned_grid2D / block<T>     src/grid2grid/grid_layout.hpp:7-63,
+ *                                                 src/grid2grid/grid2D.hpp:46-125,
+ *                                                 src/grid2grid/block.hpp:60-190
+ */
+#ifndef GRID2GRID_GB300_H
+#define GRID2GRID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define G2G_VERSION_MAJOR 0
+#define G2G_VERSION_MINOR 1
+
+/* Status codes replace the reference's exceptions (std::runtime_error from
+ * interval.cpp:5-17, grid2D.cpp:29-43, block.cpp:167-174,
+ * grid_cover.hpp:57-62, scalapack_layout.cpp:12-15,43-48) and its asserts
+ * (communication_data.cpp:227-239, grid_cover.cpp:70). */
+typedef enum g2g_status {
+    G2G_SUCCESS = 0,
+    G2G_ERROR_INVALID_ARGUMENT = 1, /* descriptor violates a layout invariant   */
+    G2G_ERROR_CUDA = 2,             /* a CUDA runtime call failed               */
+    G2G_ERROR_OUT_OF_MEMORY = 3,    /* device allocation for plan metadata      */
+    G2G_ERROR_BUDGET = 4,           /* request exceeds the server's HBM budget  */
+    G2G_ERROR_TIMEOUT = 5,          /* a bounded wait expired                   */
+    G2G_ERROR_NOT_READY = 6,        /* asynchronous result not available yet    */
+    G2G_ERROR_UNSUPPORTED = 7       /* valid request this build cannot serve    */
+} g2g_status;
+
+/* The four element types the reference instantiates (transform.cpp:206-298,
+ * mpi_type_wrapper.hpp:9-70). Complex types are {real, imag} pairs, the
+ * layout of std::complex<float> / std::complex<double>. */
+typedef enum g2g_dtype {
+    G2G_FLOAT32 = 0,    /* float                 4 bytes */
+    G2G_FLOAT64 = 1,    /* double                8 bytes */
+    G2G_COMPLEX64 = 2,  /* std::complex<float>   8 bytes */
+    G2G_COMPLEX128 = 3  /* std::complex<double> 16 bytes */
+} g2g_dtype;
+
+/* One locally stored block (block<T>, block.hpp:60-146). Its row and column
+ * intervals are the grid's intervals at (row, col). With transpose_on_copy
+ * set, the grid coordinates are those of the (already transposed) layout and
+ * the memory holds the un-transposed block, exactly as block<T> after
+ * transpose_or_conjugate (block.cpp:249-288). */
+typedef struct g2g_block_desc {
+    int32_t rank;              /* virtual rank whose local_blocks hold it   */
+    int32_t row;               /* block_coordinates::row                    */
+    int32_t col;               /* block_coordinates::col                    */
+    int32_t transpose_on_copy; /* block<T>::transpose_on_copy (0/1)         */
+    int32_t conjugate_on_copy; /* block<T>::conjugate_on_copy (0/1)         */
+    int32_t reserved;
+    int64_t stride;            /* leading dimension in elements             */
+    void *data;                /* device address of element (0,0)           */
+} g2g_block_desc;
+
+/* A grid_layout over P virtual ranks (grid_layout.hpp:7-63): the grid, the
+ * owner matrix (with optional rank reordering, grid2D.cpp:112-122) and the
+ * local blocks of ALL ranks. */
+typedef struct g2g_layout_desc {
+    int32_t n_block_rows;       /* grid2D::n_rows (number of row intervals)  */
+    int32_t n_block_cols;       /* grid2D::n_cols                            */
+    const int32_t *rows_split;  /* n_block_rows + 1 non-decreasing entries   */
+    const int32_t *cols_split;  /* n_block_cols + 1 non-decreasing entries   */
+    const int32_t *owners;      /* row-major n_block_rows x n_block_cols:
+                                   owners[i*n_block_cols + j] = ranks[i][j]  */
+    int32_t n_ranks;            /* assigned_grid2D::num_ranks()              */
+    int32_t n_reordering;       /* 0, or number of entries in `reordering`   */
+    const int32_t *reordering;  /* owner(i,j) = reordering[ranks[i][j]]      */
+    int32_t n_blocks;           /* local blocks over all virtual ranks       */
+    int32_t reserved;
+    const g2g_block_desc *blocks;
+} g2g_layout_desc;
+
+/* The (trans, alpha, beta) of transform.hpp:20-25. alpha/beta are given as
+ * {real, imag} doubles and converted to the element type (the imaginary part
+ * must be 0 for real types). (alpha, beta) == (1, 0) is a pure bit copy, as
+ * in memory_utils.hpp:92-95. trans is 'N', 'T' or 'C' (any case); 'T'/'C'
+ * transpose the initial layout first (grid_layout.hpp:18-25); the caller's
+ * descriptor is not modified. */
+typedef struct g2g_op {
+    char trans;
+    char reserved[7];
+    double alpha[2];
+    double beta[2];
+} g2g_op;
+
+/* Knobs of the gather-scatter kernels. Zero fields mean "library default".
+ * g2g_plan_autotune picks them by measurement. */
+typedef struct g2g_tuning {
+    int32_t tile_bytes;       /* target bytes per non-transposed tile       */
+    int32_t tile_dim;         /* edge (elements) of a transposed tile: 16/32/64 */
+    int32_t ctas_per_sm;      /* persistent grid = ctas_per_sm x SM count   */
+    int32_t threads;          /* threads per CTA: 128, 256 or 512           */
+    int32_t unroll;           /* 16-byte chunks in flight per thread: 1,2,4,8 */
+    int32_t reserved[3];
+} g2g_tuning;
+
+typedef struct g2g_plan_info {
+    int32_t n_pairs;          /* layout pairs in the plan                    */
+    int32_t n_ranks;          /* largest virtual-rank count over the pairs   */
+    int64_t n_pieces;         /* non-empty (initial block x final block) pieces */
+    int64_t n_tiles;          /* work items of the gather-scatter kernel     */
+    int64_t bytes_moved;      /* sum of m*n*sizeof(T) over the pairs         */
+    int64_t bytes_min_traffic;/* 2x bytes_moved (3x for pieces with beta!=0) */
+    int64_t metadata_bytes;   /* device memory held by the plan              */
+    int32_t graph_captured;   /* 1 after g2g_plan_capture_graph              */
+    int32_t reserved;
+    g2g_tuning tuning;        /* knobs in effect                             */
+} g2g_plan_info;
+
+typedef struct g2g_plan g2g_plan;
+
+/* ---- errors and version ------------------------------------------------ */
+const char *g2g_last_error_string(void);
+const char *g2g_version_string(void);
+
+/* ---- planning ---------------------------------------------------------- */
+
+/* Plans one transform (transform.hpp:13-25; utils::prepare_to_send/recv,
+ * utils.hpp:146-212). Host side: validates both descriptors and builds the
+ * per-layout block tables. Device side (stream-ordered, no host sync): the
+ * grid cover by a parallel merge of the split vectors, per-block piece counts,
+ * a scan, and the emission of the piece and tile work lists. `op` may be NULL
+ * (= 'N', 1, 0). */
+g2g_status g2g_plan_create(const g2g_layout_desc *initial,
+                           const g2g_layout_desc *final_,
+                           g2g_dtype dtype, const g2g_op *op,
+                           void *stream, g2g_plan **plan);
+
+/* Plans n_pairs transforms executed together, the vector overloads
+ * (transform.hpp:30-43) and transformer<T>::transform (transformer.hpp:44-53).
+ * Unlike the reference, each pair may have its own dtype. ops may be NULL.
+ * Destinations of different pairs must not overlap. */
+g2g_status g2g_plan_create_batch(int32_t n_pairs,
+                                 const g2g_layout_desc *initials,
+                                 const g2g_layout_desc *finals,
+                                 const g2g_dtype *dtypes, const g2g_op *ops,
+                                 void *stream, g2g_plan **plan);
+
+/* Runs the plan's gather-scatter on `stream` (exchange_async,
+ * transform.cpp:41-124, as one kernel). Replays the captured graph if
+ * g2g_plan_capture_graph was called. */
+g2g_status g2g_plan_execute(g2g_plan *plan, void *stream);
+
+/* Captures one execution into a CUDA graph; later executes replay it. */
+g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream);
+
+g2g_status g2g_plan_set_tuning(g2g_plan *plan, const g2g_tuning *tuning);
+
+/* Times candidate tunings on `stream` (each executes the plan, so the
+ * destination is written) and keeps the fastest; *best may be NULL. */
+g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters,
+                             g2g_tuning *best);
+
+g2g_status g2g_plan_get_info(const g2g_plan *plan, g2g_plan_info *info);
+
+/* Frees the plan's device metadata after work queued on the plan's last
+ * stream has finished (stream-ordered free). */
+g2g_status g2g_plan_destroy(g2g_plan *plan);
+
+/* ---- one-shot transform ------------------------------------------------ */
+
+/* plan + execute + destroy: the reference's transform() call
+ * (transform.cpp:126-164), which also re-plans on every call. */
+g2g_status g2g_transform(const g2g_layout_desc *initial,
+                         const g2g_layout_desc *final_, g2g_dtype dtype,
+                         const g2g_op *op, void *stream);
+
+g2g_status g2g_transform_batch(int32_t n_pairs,
+                               const g2g_layout_desc *initials,
+                               const g2g_layout_desc *finals,
+                               const g2g_dtype *dtypes, const g2g_op *ops,
+                               void *stream);
+
+/* ---- grid cover -------------------------------------------------------- */
+
+/* grid_cover of two split vectors (get_decomp_cover, grid_cover.cpp:54-121),
+ * computed on the device by a parallel merge. Host arrays in and out:
+ * for k in [0, n_a-1): start_index[k] = max i with b[i] <= a[k],
+ * end_index[k] = min i with b[i] >= a[k+1]. Requires a[0] == b[0] and
+ * a[n_a-1] == b[n_b-1]. Synchronises `stream`. */
+g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a,
+                          const int32_t *splits_b, int32_t n_b,
+                          int32_t *start_index, int32_t *end_index,
+                          void *stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* GRID2GRID_GB300_H */
