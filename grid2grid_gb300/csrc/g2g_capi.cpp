@@ -139,7 +139,7 @@ g2g_status check_splits(const int32_t *s, int n, const char *what, const char *w
 // Reads and validates one layout descriptor. `P` is the number of virtual
 // ranks of the transform (the communicator size).
 g2g_status load_layout(const g2g_layout_desc *d, const char *which, int P, bool is_final,
-                       HLayout &L) {
+                       int align, HLayout &L) {
     if (!d)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout descriptor is NULL", which);
     G2G_TRY(check_splits(d->rows_split, d->n_block_rows, "rows", which));
@@ -218,6 +218,11 @@ g2g_status load_layout(const g2g_layout_desc *d, const char *which, int P, bool 
                 return fail(G2G_ERROR_INVALID_ARGUMENT,
                             "%s layout: block (%d, %d) has a NULL data pointer", which,
                             bd.row, bd.col);
+            if (((uintptr_t)bd.data) % (uintptr_t)align != 0)
+                return fail(G2G_ERROR_INVALID_ARGUMENT,
+                            "%s layout: block (%d, %d) data pointer is not aligned to its "
+                            "element type (%d bytes)",
+                            which, bd.row, bd.col, align);
             if (bd.stride < 1 || (scols > 1 && bd.stride < srows))
                 return fail(G2G_ERROR_INVALID_ARGUMENT,
                             "%s layout: block (%d, %d) has stride %lld < %lld stored rows",
@@ -278,11 +283,11 @@ struct PairHost {
 g2g_tuning default_tuning() {
     g2g_tuning t;
     std::memset(&t, 0, sizeof(t));
-    t.tile_bytes = 32 * 1024;
+    t.tile_bytes = 64 * 1024;
     t.tile_dim = 32;
     t.ctas_per_sm = 4;
     t.threads = 256;
-    t.unroll = 4;
+    t.unroll = 2;
     return t;
 }
 
@@ -376,8 +381,10 @@ g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int 
     if (!di || !df)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "layout descriptor is NULL");
     const int P = std::max(1, std::max(di->n_ranks, df->n_ranks));
-    G2G_TRY(load_layout(di, "initial", P, false, p.a));
-    G2G_TRY(load_layout(df, "final", P, true, p.b));
+    // element alignment: that of the real component (float or double)
+    const int align = (dtype == G2G_FLOAT32 || dtype == G2G_COMPLEX64) ? 4 : 8;
+    G2G_TRY(load_layout(di, "initial", P, false, align, p.a));
+    G2G_TRY(load_layout(df, "final", P, true, align, p.b));
     char trans = 'N';
     if (op) {
         trans = (char)std::toupper((unsigned char)op->trans);
@@ -497,6 +504,27 @@ void assemble(g2g_plan &pl) {
         else
             pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0);
     }
+}
+
+// Makes the device that holds the plan's blocks current for this library's
+// runtime (callers such as torch keep their own current-device state).
+g2g_status bind_device(g2g_plan &pl) {
+    for (const PairHost &p : pl.host)
+        for (const HLayout *L : {&p.a, &p.b})
+            for (const HBlock &b : L->blocks) {
+                if (!b.data)
+                    continue;
+                cudaPointerAttributes attr;
+                G2G_CUDA(cudaPointerGetAttributes(&attr, (const void *)(uintptr_t)b.data));
+                if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+                    return fail(G2G_ERROR_INVALID_ARGUMENT,
+                                "block data at %p is not device memory (use the host-layout "
+                                "transform for host buffers)",
+                                (void *)(uintptr_t)b.data);
+                G2G_CUDA(cudaSetDevice(attr.device));
+                return G2G_SUCCESS;
+            }
+    return G2G_SUCCESS;
 }
 
 // Allocates device memory, uploads, runs the device planner, waits for it.
@@ -645,12 +673,21 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
         pl->n_ranks = std::max(pl->n_ranks, std::max(inits[k].n_ranks, finals[k].n_ranks));
     }
     assemble(*pl);
-    g2g_status st = plan_on_device(*pl);
+    g2g_status st = bind_device(*pl);
+    if (st == G2G_SUCCESS)
+        st = plan_on_device(*pl);
     if (st != G2G_SUCCESS) {
         g2g_plan_destroy(pl);
         return st;
     }
     G2G_CUDA(cudaEventCreateWithFlags(&pl->done, cudaEventDisableTiming));
+    // Large tiles keep enough bytes in flight with fewer, deeper threads;
+    // small tiles (many small pieces) want more resident CTAs instead
+    // (measured on GB300 for 8 KB and ~27 KB average tiles).
+    if (pl->n_tiles > 0 && pl->bytes_moved / pl->n_tiles >= 24 * 1024 && pl->paths == 1) {
+        pl->tuning.unroll = 4;
+        pl->tuning.ctas_per_sm = 8;
+    }
     *out = pl;
     return G2G_SUCCESS;
 }
@@ -683,6 +720,7 @@ g2g_status g2g_plan_execute(g2g_plan *plan, void *stream) {
     if (!plan)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "plan is NULL");
     cudaStream_t s = (cudaStream_t)stream;
+    G2G_CUDA(cudaSetDevice(plan->device));
     if (plan->n_tiles > 0) {
         if (plan->graph && plan->graph_stream == s) {
             G2G_CUDA(cudaGraphLaunch(plan->graph, s));
@@ -702,6 +740,7 @@ g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream) {
     if (!s)
         return fail(G2G_ERROR_INVALID_ARGUMENT,
                     "graph capture needs a non-default stream");
+    G2G_CUDA(cudaSetDevice(plan->device));
     if (plan->graph) {
         cudaGraphExecDestroy(plan->graph);
         plan->graph = nullptr;
@@ -830,6 +869,7 @@ g2g_status g2g_plan_destroy(g2g_plan *plan) {
         cudaGraphExecDestroy(plan->graph);
     if (plan->dmem) {
         DeviceState *ds = nullptr;
+        cudaSetDevice(plan->device);
         if (device_state(&ds, nullptr) == G2G_SUCCESS) {
             // free after the last execution that used the plan
             if (plan->done && plan->last_stream != nullptr)

@@ -103,67 +103,81 @@ __device__ __forceinline__ uint4 funnel_words(uint4 lo, uint4 hi, uint32_t q) {
 }
 
 // ------------------------------------------------------------ plain copy tile
+// Lanes of a warp form groups of `lpc` lanes (a power of two); a group walks
+// one column of the tile in 16-byte chunks aligned to the DESTINATION.
+//  * aligned tiles (source and destination at the same 16-byte phase in every
+//    column): lane kl copies chunks kl, kl + lpc, ... with one 128-bit load and
+//    one 128-bit store each;
+//  * otherwise every lane loads the aligned source block under its chunk and
+//    takes the next block from the next lane (warp shuffle) to funnel the
+//    window into place; the group's last lane only supplies that block, so a
+//    group stores lpc - 1 chunks per step and its last chunk is loaded again
+//    by the group's first lane on the next step.
+// A column of a tile is at most 4 KB (tiles are cut at 4096 / sizeof(T)
+// rows), so per-chunk arithmetic is 32-bit, relative to the column's first
+// aligned destination chunk. Only 16-byte blocks overlapping the column are
+// read, so no access leaves the pages the column lives in; stores cover
+// exactly the column (word-masked head and tail chunks).
 template <int THREADS, int U>
 __device__ __forceinline__ void copy_tile(const Tile &t) {
     constexpr int NWARP = THREADS / 32;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int esz = kind_esz(t.kind);
-    const long long L = (long long)t.rows * esz; // bytes per column
+    const int L = t.rows * esz; // bytes per column, <= 4096
     if (L <= 0 || t.cols <= 0)
         return;
-    // destination-aligned 16-byte chunks a column can touch
-    const int cpc = (int)((L + 27) >> 4);
+    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    // destination chunks a column touches (exact if every column starts at
+    // the same 16-byte phase, else the bound over the four phases)
+    const int cpc = ((t.dst_ld & 15) == 0) ? (((int)(t.dst & 15u) + L + 15) >> 4)
+                                           : ((L + 27) >> 4);
+    // lanes per column: the smallest power of two whose step covers cpc
     int lpc_shift = 0;
-    while ((1 << lpc_shift) < cpc && lpc_shift < 5)
+    while (lpc_shift < 5 && ((1 << lpc_shift) - (aligned ? 0 : 1)) < cpc)
         ++lpc_shift;
-    const int lpc = 1 << lpc_shift;          // lanes per column
-    const int cpw = 32 >> lpc_shift;         // columns per warp step
+    if (!aligned && lpc_shift == 0)
+        lpc_shift = 1;
+    const int lpc = 1 << lpc_shift;
+    const int step = aligned ? lpc : lpc - 1; // chunks stored per group step
+    const int cpw = 32 >> lpc_shift;          // columns per warp step
     const int sub = lane >> lpc_shift;
     const int kl = lane & (lpc - 1);
-    const bool last_in_group = kl == lpc - 1;
+    const bool stores = aligned || kl != lpc - 1;
     const int col_step = NWARP * cpw;
     const int warp_col0 = warp * cpw;
     const int ncolit =
         t.cols > warp_col0 ? (t.cols - warp_col0 + col_step - 1) / col_step : 0;
-    const int nkit = (cpc + lpc - 1) >> lpc_shift;
+    const int nkit = (cpc + step - 1) / step;
     const int my_col0 = warp_col0 + sub;
 
     int colit = 0, kit = 0;
     while (colit < ncolit) { // warp-uniform
-        uint4 lo[U], hx[U];
+        uint4 lo[U];
         uint64_t chunk[U];
-        uint32_t q[U], wm[U];
+        uint32_t qm[U]; // bits 0-3 store mask, bits 4-5 word shift
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int c = my_col0 + colit * col_step;
             const bool colok = (colit < ncolit) && (c < t.cols);
             const uint64_t d = t.dst + (uint64_t)((long long)c * t.dst_ld);
             const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
-            const uint64_t ch = (d & ~15ull) + ((uint64_t)(kl + (kit << lpc_shift)) << 4);
-            const uint64_t vlo = ch > d ? ch : d;
-            const uint64_t dend = d + (uint64_t)L;
-            const uint64_t vhi = (ch + 16 < dend) ? ch + 16 : dend;
-            uint32_t m = 0;
-            if (colok && vlo < vhi) {
-                const uint32_t w0 = (uint32_t)(vlo - ch) >> 2;
-                const uint32_t w1 = (uint32_t)(vhi - ch) >> 2;
-                m = ((1u << w1) - 1u) & ~((1u << w0) - 1u);
-            }
-            const uint64_t win = ch + (s - d); // source address of the chunk's first byte
-            const uint32_t shb = (uint32_t)(win & 15u);
-            const uint64_t la = win - shb;
-            const uint64_t send = s + (uint64_t)L;
-            // load only 16-byte blocks that overlap the source column, so no
-            // access leaves the pages the column lives in
-            const bool need_lo = colok && (la < send) && (la + 16 > s);
-            lo[u] = need_lo ? ldg_v4(la) : make_uint4(0u, 0u, 0u, 0u);
-            const bool need_hi =
-                colok && last_in_group && shb != 0 && (la + 16 < send) && (la + 32 > s);
-            hx[u] = need_hi ? ldg_v4(la + 16) : make_uint4(0u, 0u, 0u, 0u);
-            chunk[u] = ch;
-            q[u] = shb >> 2;
-            wm[u] = m;
+            const int d0 = (int)(d & 15u);        // destination phase
+            const uint64_t sa = s - (uint64_t)d0; // source byte of chunk 0's first byte
+            const int sh = (int)(sa & 15u);       // source phase vs. destination
+            const int rel = (kl + kit * step) << 4;
+            const int lo_lim = sh + d0, hi_lim = sh + d0 + L;
+            const bool need = colok && rel < hi_lim && rel + 16 > lo_lim;
+            lo[u] = need ? ldg_v4(sa - (uint64_t)sh + (uint64_t)rel)
+                         : make_uint4(0u, 0u, 0u, 0u);
+            // words of this chunk inside the destination column [d0, d0 + L)
+            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
+            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
+            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
+            uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
+            m = (colok && stores) ? m : 0u;
+            chunk[u] = d - (uint64_t)d0 + (uint64_t)rel;
+            qm[u] = m | ((uint32_t)(sh >> 2) << 4);
             if (++kit == nkit) {
                 kit = 0;
                 ++colit;
@@ -171,14 +185,18 @@ __device__ __forceinline__ void copy_tile(const Tile &t) {
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            uint4 nb;
-            nb.x = __shfl_down_sync(0xffffffffu, lo[u].x, 1);
-            nb.y = __shfl_down_sync(0xffffffffu, lo[u].y, 1);
-            nb.z = __shfl_down_sync(0xffffffffu, lo[u].z, 1);
-            nb.w = __shfl_down_sync(0xffffffffu, lo[u].w, 1);
-            const uint4 hi = last_in_group ? hx[u] : nb;
-            const uint4 o = q[u] ? funnel_words(lo[u], hi, q[u]) : lo[u];
-            const uint32_t m = wm[u];
+            uint4 o = lo[u];
+            if (!aligned) { // tile-uniform
+                uint4 nb;
+                nb.x = __shfl_down_sync(0xffffffffu, lo[u].x, 1);
+                nb.y = __shfl_down_sync(0xffffffffu, lo[u].y, 1);
+                nb.z = __shfl_down_sync(0xffffffffu, lo[u].z, 1);
+                nb.w = __shfl_down_sync(0xffffffffu, lo[u].w, 1);
+                const uint32_t q = qm[u] >> 4;
+                if (q)
+                    o = funnel_words(lo[u], nb, q);
+            }
+            const uint32_t m = qm[u] & 15u;
             if (m == 0xFu) {
                 st_v4(chunk[u], o);
             } else if (m) {
@@ -467,11 +485,17 @@ __device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *p
 // register cost of the scaled complex arithmetic.
 enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
 
-// At least 1024 resident threads per SM (64 registers a thread): with U
-// 16-byte loads in flight per thread that keeps >= 32 KB of reads in flight
-// per SM, what HBM3e needs at this SM count.
+// Resident threads per SM: 1024 (64 registers each) for shallow unrolling,
+// 512 (up to 128 registers) for U >= 4, so every variant keeps
+// U x 16 B x threads >= 32 KB of reads in flight per SM without spilling.
+template <int U, int THREADS> struct MinBlocks {
+    static constexpr int value = ((U <= 2 ? 1024 : 512) / THREADS) > 0
+                                     ? ((U <= 2 ? 1024 : 512) / THREADS)
+                                     : 1;
+};
+
 template <int THREADS, int U, int PATHS>
-__global__ void __launch_bounds__(THREADS, 1024 / THREADS)
+__global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
     scatter_kernel(const Tile *__restrict__ tiles, const long long *__restrict__ n_tiles_p,
                    long long capacity, const PairInfo *__restrict__ pairs, int td) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -479,6 +503,8 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS)
     if (n > capacity)
         n = capacity;
     for (long long ti = blockIdx.x; ti < n; ti += gridDim.x) {
+        if (threadIdx.x == 0 && ti + gridDim.x < n)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(tiles + ti + gridDim.x));
         const Tile t = tiles[ti];
         const uint32_t k = t.kind;
         if ((PATHS & PATH_COPY) && !(k & (KIND_TRANS | KIND_SCALED)))

@@ -94,7 +94,10 @@ def gpu_run(inits, finals, init_arenas, final_arenas, ops=None, how="transform",
     n = len(inits)
     dts = (C.c_int * n)(*[L.dtype for L in inits])
     opa = make_ops(ops, n)
-    s = torch.cuda.current_stream() if stream is None else stream
+    if stream is None:
+        # graph capture needs a real (non-legacy-default) stream
+        stream = torch.cuda.Stream() if how == "graph" else torch.cuda.current_stream()
+    s = stream
     sp = C.c_void_p(s.cuda_stream)
     if how == "transform":
         assert n == 1
