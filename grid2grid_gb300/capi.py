@@ -77,7 +77,8 @@ class Tuning(C.Structure):
         ("ctas_per_sm", C.c_int32),
         ("threads", C.c_int32),
         ("unroll", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("stages", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -91,7 +92,7 @@ class PlanInfo(C.Structure):
         ("bytes_min_traffic", C.c_int64),
         ("metadata_bytes", C.c_int64),
         ("graph_captured", C.c_int32),
-        ("reserved", C.c_int32),
+        ("device_status", C.c_int32),
         ("tuning", Tuning),
     ]
 

@@ -288,6 +288,7 @@ g2g_tuning default_tuning() {
     t.ctas_per_sm = 4;
     t.threads = 256;
     t.unroll = 2;
+    t.stages = 3;
     return t;
 }
 
@@ -300,6 +301,7 @@ g2g_tuning merge_tuning(const g2g_tuning &base, const g2g_tuning *over) {
     if (over->ctas_per_sm) t.ctas_per_sm = over->ctas_per_sm;
     if (over->threads) t.threads = over->threads;
     if (over->unroll) t.unroll = over->unroll;
+    if (over->stages) t.stages = over->stages;
     return t;
 }
 
@@ -309,10 +311,12 @@ g2g_status check_tuning(const g2g_tuning &t) {
                     t.tile_bytes);
     if (t.tile_dim != 16 && t.tile_dim != 32 && t.tile_dim != 64)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_dim must be 16, 32 or 64");
-    if (t.threads != 128 && t.threads != 256 && t.threads != 512)
-        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: threads must be 128, 256 or 512");
-    if (t.unroll != 1 && t.unroll != 2 && t.unroll != 4 && t.unroll != 8)
-        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: unroll must be 1, 2, 4 or 8");
+    if (t.threads != 256 && t.threads != 512)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: threads must be 256 or 512");
+    if (t.unroll != 1 && t.unroll != 2 && t.unroll != 4)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: unroll must be 1, 2 or 4");
+    if (t.stages != -1 && (t.stages < 2 || t.stages > 4))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: stages must be -1 or 2..4");
     if (t.ctas_per_sm < 1 || t.ctas_per_sm > 32)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ctas_per_sm outside [1, 32]");
     return G2G_SUCCESS;
@@ -577,6 +581,7 @@ g2g_status plan_on_device(g2g_plan &pl) {
     d.n_tiles = (long long *)(base + o_counters);
     d.n_pieces = (unsigned long long *)(base + o_counters + 8);
     d.overflow = (int *)(base + o_counters + 16);
+    d.status = (int *)(base + o_counters + 24);
     d.tiles = (g2g::Tile *)(base + o_tiles);
     d.tile_capacity = capacity;
     d.max_cells_per_pair = pl.max_cells_per_pair;
@@ -630,11 +635,15 @@ g2g_status plan_on_device(g2g_plan &pl) {
     return G2G_SUCCESS;
 }
 
+// Largest dynamic shared memory a CTA can opt into on sm_100-class GPUs.
+constexpr size_t kMaxSmemPerCta = 227 * 1024;
+
 g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     g2g::ScatterConfig c;
     c.threads = pl.tuning.threads;
     c.unroll = pl.tuning.unroll;
     c.ctas_per_sm = pl.tuning.ctas_per_sm;
+    c.sm_count = pl.sm_count;
     c.tile_dim = pl.tuning.tile_dim;
     long long g = (long long)pl.sm_count * pl.tuning.ctas_per_sm;
     if (g > pl.n_tiles)
@@ -642,7 +651,16 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     c.grid = (int)std::max<long long>(g, 1);
     c.smem_bytes = pl.max_trans_esz ? g2g::transpose_smem_bytes(c.tile_dim, pl.max_trans_esz)
                                     : 0;
+    c.trans_bytes = c.smem_bytes;
     c.paths = pl.paths ? pl.paths : 1;
+    c.stages = 0;
+    if ((c.paths & 1) && pl.tuning.stages >= 2) {
+        c.stage_bytes = g2g::stage_bytes_for(pl.tuning.tile_bytes);
+        int st = pl.tuning.stages;
+        while (st >= 2 && 128 + (size_t)st * c.stage_bytes + c.trans_bytes > kMaxSmemPerCta)
+            --st;
+        c.stages = st >= 2 ? st : 0;
+    }
     return c;
 }
 
@@ -688,6 +706,7 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
         pl->tuning.unroll = 4;
         pl->tuning.ctas_per_sm = 8;
     }
+    (void)0;
     *out = pl;
     return G2G_SUCCESS;
 }
@@ -793,25 +812,30 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
     const int tile_bytes_opts[] = {16 * 1024, 32 * 1024, 64 * 1024};
     const int tile_dim_opts[] = {32, 64};
     const int threads_opts[] = {256, 512};
-    const int unroll_opts[] = {2, 4, 8};
+    const int unroll_opts[] = {2, 4};
     const int ctas_opts[] = {2, 4, 8};
+    const int stage_opts[] = {-1, 2, 3, 4};
     for (int tb : tile_bytes_opts)
         for (int td : tile_dim_opts) {
             if (!plan->any_trans && td != start.tile_dim)
                 continue;
             for (int th : threads_opts)
                 for (int u : unroll_opts)
-                    for (int c : ctas_opts) {
-                        if (th * c > 2048)
-                            continue;
-                        g2g_tuning t = start;
-                        t.tile_bytes = tb;
-                        t.tile_dim = td;
-                        t.threads = th;
-                        t.unroll = u;
-                        t.ctas_per_sm = c;
-                        cands.push_back(t);
-                    }
+                    for (int c : ctas_opts)
+                        for (int sg : stage_opts) {
+                            if (th * c > 2048)
+                                continue;
+                            if (sg != -1 && !(plan->paths & 1))
+                                continue;
+                            g2g_tuning t = start;
+                            t.tile_bytes = tb;
+                            t.tile_dim = td;
+                            t.threads = th;
+                            t.unroll = u;
+                            t.ctas_per_sm = c;
+                            t.stages = sg;
+                            cands.push_back(t);
+                        }
         }
     cudaEvent_t e0, e1;
     G2G_CUDA(cudaEventCreate(&e0));
@@ -858,6 +882,13 @@ g2g_status g2g_plan_get_info(const g2g_plan *plan, g2g_plan_info *info) {
     info->metadata_bytes = (int64_t)plan->dmem_bytes;
     info->graph_captured = plan->graph ? 1 : 0;
     info->tuning = plan->tuning;
+    if (plan->dev.status) {
+        G2G_CUDA(cudaSetDevice(plan->device));
+        G2G_CUDA(cudaEventSynchronize(plan->done));
+        int st = 0;
+        G2G_CUDA(cudaMemcpy(&st, plan->dev.status, sizeof(int), cudaMemcpyDeviceToHost));
+        info->device_status = st;
+    }
     return G2G_SUCCESS;
 }
 

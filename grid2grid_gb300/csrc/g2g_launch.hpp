@@ -20,6 +20,7 @@ struct PlanDevice {
     long long *n_tiles = nullptr;      // device scalar: tiles in the work list
     unsigned long long *n_pieces = nullptr;
     int *overflow = nullptr;           // device flag: tile capacity exceeded
+    int *status = nullptr;             // device flag: kernel error (bounded wait expired)
     long long tile_capacity = 0;
     long long max_cells_per_pair = 0;
 };
@@ -38,10 +39,21 @@ struct ScatterConfig {
     int unroll = 4;          // 1, 2, 4 or 8
     int grid = 0;            // CTAs (persistent); 0 = SM count x ctas_per_sm
     int ctas_per_sm = 4;
+    int sm_count = 0;        // for the residency clamp of the persistent grid
     int tile_dim = 32;       // transposed tile edge (16, 32 or 64)
     size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled
+    int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
+    int stage_bytes = 0;     // bytes per stage
+    size_t trans_bytes = 0;  // shared memory for direct transposed / scaled tiles
 };
+
+// Stage size that holds any plain tile of `tile_bytes` whose columns are at
+// least 256 bytes: columns are staged as their 16-byte aligned cover.
+int stage_bytes_for(int tile_bytes);
+// Dynamic shared memory of the staged kernel.
+size_t staged_smem_bytes(const ScatterConfig &cfg);
+
 
 // Shared memory a transposed tile of edge `tile_dim` with elements of `esz`
 // bytes needs.

@@ -12,7 +12,9 @@
 //     intervals ib of the parts whose ia == k.
 //  2. cell_tiles_kernel    one thread per (row part, col part) cell, i.e. per
 //     piece of the reference's utils::decompose_block (utils.hpp:10-65):
-//     the number of tiles the piece is cut into.
+//     the number of tiles the piece is cut into. Cells are numbered column
+//     part by column part (row parts fastest), which fixes the order of the
+//     work list.
 //  3. scan_*               exclusive scan of the tile counts over all cells of
 //     all pairs (three-phase: per-CTA sums, scan of sums, apply).
 //  4. emit_tiles_kernel    one warp per cell writes the cell's tiles, with the
@@ -118,8 +120,11 @@ __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pair
     unsigned long long local_pieces = 0;
     for (long long cidx = (long long)blockIdx.x * blockDim.x + threadIdx.x; cidx < n_cells;
          cidx += (long long)gridDim.x * blockDim.x) {
-        int u = (int)(cidx / ncp);
-        int v = (int)(cidx - (long long)u * ncp);
+        // column-strip order: the row parts of one column part are
+        // consecutive, so pieces that share destination (and source) columns
+        // are in flight together and their boundary sectors meet in L2
+        int v = (int)(cidx / nrp);
+        int u = (int)(cidx - (long long)v * nrp);
         Part pr = parts[p.row_parts + u];
         Part pc = parts[p.col_parts + v];
         long long cnt = 0;
@@ -243,8 +248,8 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
     const long long warps_total = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long cidx = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
          cidx < n_cells; cidx += warps_total) {
-        int u = (int)(cidx / ncp);
-        int v = (int)(cidx - (long long)u * ncp);
+        int v = (int)(cidx / nrp); // column-strip order, as in cell_tiles_kernel
+        int u = (int)(cidx - (long long)v * nrp);
         Part pr = parts[p.row_parts + u];
         Part pc = parts[p.col_parts + v];
         if (pr.len <= 0 || pc.len <= 0)

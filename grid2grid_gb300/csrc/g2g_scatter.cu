@@ -209,6 +209,222 @@ __device__ __forceinline__ void copy_tile(const Tile &t) {
     }
 }
 
+// ------------------------------------------------------------ TMA staging
+// The staged kernel keeps several tiles in flight per CTA without holding
+// their data in registers: one lane per column issues a 1-D TMA bulk copy
+// (cp.async.bulk) of the column's 16-byte aligned cover into a ring of
+// shared-memory stages; an mbarrier per stage counts the bytes landed. The
+// CTA then shifts each destination chunk out of shared memory and stores it
+// with 128-bit stores.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Waits for a stage, giving up after `limit_ns` (returns false then).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
+                                                  uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const uint64_t t0 = global_timer_ns();
+    for (uint32_t i = 0; i < (1u << 30); ++i) {
+        if (mbar_try_wait(bar, parity))
+            return true;
+        if (global_timer_ns() - t0 > limit_ns)
+            return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, uint64_t src, uint32_t bytes,
+                                          uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                 "[%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ uint4 lds_v4(uint32_t a) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(a));
+    return v;
+}
+__device__ __forceinline__ uint2 lds_v2(uint32_t a) {
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+
+// Bytes one staged column takes: its 16-byte aligned cover, at most
+// round_up(L, 16) + 16.
+__device__ __forceinline__ int staged_pitch(int L) { return ((L + 15) & ~15) + 16; }
+
+// Plain tiles whose columns are long enough for bulk copies to pay off and
+// whose columns fit one stage.
+__device__ __forceinline__ bool tma_eligible(const Tile &t, int stage_bytes) {
+    if (t.kind & (KIND_TRANS | KIND_SCALED))
+        return false;
+    const int L = t.rows * kind_esz(t.kind);
+    return L >= 256 && (long long)t.cols * staged_pitch(L) <= (long long)stage_bytes;
+}
+
+// Warp 0: start the bulk copies of tile `ti` into `stage` (nothing when the
+// tile is past the end or not eligible).
+__device__ __forceinline__ void issue_stage(const Tile *__restrict__ tiles, long long ti,
+                                            long long n, unsigned char *stage, uint32_t bar,
+                                            int stage_bytes) {
+    if (ti >= n)
+        return;
+    const int lane = threadIdx.x & 31;
+    const Tile t = tiles[ti];
+    if (!tma_eligible(t, stage_bytes))
+        return;
+    const int L = t.rows * kind_esz(t.kind);
+    const int pitch = staged_pitch(L);
+    uint32_t total = 0;
+    for (int c = lane; c < t.cols; c += 32) {
+        const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+        total += (uint32_t)(((s + (uint64_t)L + 15u) & ~15ull) - (s & ~15ull));
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        total += __shfl_xor_sync(0xffffffffu, total, off);
+    if (lane == 0) {
+        // order earlier generic-proxy reads of this stage before the async writes
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, total);
+    }
+    __syncwarp();
+    const uint32_t sbase = smem_addr(stage);
+    for (int c = lane; c < t.cols; c += 32) {
+        const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+        const uint64_t a0 = s & ~15ull;
+        const uint32_t len = (uint32_t)(((s + (uint64_t)L + 15u) & ~15ull) - a0);
+        bulk_load(sbase + (uint32_t)(c * pitch), a0, len, bar);
+    }
+}
+
+// All threads: write tile t from its staged columns. Column c's cover starts
+// at stage + c * pitch and holds source byte x at offset x - (s & ~15); the
+// destination chunk at d - d0 + rel reads its words at
+// c * pitch + (s & 15) - d0 + rel. Only words of the destination column are
+// read and written.
+template <int THREADS, int U>
+__device__ __forceinline__ void consume_stage(const Tile &t, const unsigned char *stage) {
+    constexpr int NWARP = THREADS / 32;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int L = t.rows * kind_esz(t.kind);
+    const int pitch = staged_pitch(L);
+    const int cpc = ((t.dst_ld & 15) == 0) ? (((int)(t.dst & 15u) + L + 15) >> 4)
+                                           : ((L + 27) >> 4);
+    int lpc_shift = 0;
+    while (lpc_shift < 5 && (1 << lpc_shift) < cpc)
+        ++lpc_shift;
+    const int lpc = 1 << lpc_shift;
+    const int cpw = 32 >> lpc_shift;
+    const int sub = lane >> lpc_shift;
+    const int kl = lane & (lpc - 1);
+    const int col_step = NWARP * cpw;
+    const int warp_col0 = warp * cpw;
+    const int ncolit =
+        t.cols > warp_col0 ? (t.cols - warp_col0 + col_step - 1) / col_step : 0;
+    const int nkit = (cpc + lpc - 1) >> lpc_shift;
+    const int my_col0 = warp_col0 + sub;
+    const uint32_t sbase = smem_addr(stage);
+
+    int colit = 0, kit = 0;
+    while (colit < ncolit) {
+        uint4 v[U];
+        uint64_t chunk[U];
+        uint32_t wm[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = my_col0 + colit * col_step;
+            const bool colok = (colit < ncolit) && (c < t.cols);
+            const uint64_t d = t.dst + (uint64_t)((long long)c * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+            const int d0 = (int)(d & 15u);
+            const int off0 = (int)(s & 15u) - d0;
+            const int rel = (kl + (kit << lpc_shift)) << 4;
+            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
+            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
+            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
+            uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
+            m = colok ? m : 0u;
+            const uint32_t sp = sbase + (uint32_t)(c * pitch + off0 + rel);
+            uint4 x = make_uint4(0u, 0u, 0u, 0u);
+            if (m == 0xFu) {
+                if ((off0 & 15) == 0) {
+                    x = lds_v4(sp);
+                } else if ((off0 & 7) == 0) {
+                    const uint2 a = lds_v2(sp), b = lds_v2(sp + 8);
+                    x = make_uint4(a.x, a.y, b.x, b.y);
+                } else {
+                    x = make_uint4(lds_u32(sp), lds_u32(sp + 4), lds_u32(sp + 8),
+                                   lds_u32(sp + 12));
+                }
+            } else if (m) {
+                if (m & 1u) x.x = lds_u32(sp);
+                if (m & 2u) x.y = lds_u32(sp + 4);
+                if (m & 4u) x.z = lds_u32(sp + 8);
+                if (m & 8u) x.w = lds_u32(sp + 12);
+            }
+            v[u] = x;
+            chunk[u] = d - (uint64_t)d0 + (uint64_t)rel;
+            wm[u] = m;
+            if (++kit == nkit) {
+                kit = 0;
+                ++colit;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t m = wm[u];
+            const uint4 o = v[u];
+            if (m == 0xFu) {
+                st_v4(chunk[u], o);
+            } else if (m) {
+                if (m & 1u) st_u32(chunk[u], o.x);
+                if (m & 2u) st_u32(chunk[u] + 4, o.y);
+                if (m & 4u) st_u32(chunk[u] + 8, o.z);
+                if (m & 8u) st_u32(chunk[u] + 12, o.w);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------ plain transposed tile
 template <typename W, int NWE> struct ElemW {
     W w[NWE];
@@ -498,7 +714,7 @@ template <int THREADS, int U, int PATHS>
 __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
     scatter_kernel(const Tile *__restrict__ tiles, const long long *__restrict__ n_tiles_p,
                    long long capacity, const PairInfo *__restrict__ pairs, int td) {
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     long long n = *n_tiles_p;
     if (n > capacity)
         n = capacity;
@@ -516,18 +732,117 @@ __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
     }
 }
 
-template <int THREADS, int U, int PATHS>
-cudaError_t launch_t(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
-    auto k = scatter_kernel<THREADS, U, PATHS>;
-    if (cfg.smem_bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)cfg.smem_bytes);
+// The staged variant: a ring of S shared-memory stages filled by TMA bulk
+// copies (see issue_stage / consume_stage); tiles that are not eligible for
+// staging (short columns, transposed, scaled) run on the direct paths in the
+// same loop. Every wait is bounded: on expiry the CTA records the error in
+// *status, waits (bounded) for its other stages and returns.
+constexpr uint64_t STAGE_WAIT_LIMIT_NS = 2000000000ull; // 2 s
+
+template <int THREADS, int U, int PATHS, int S>
+__global__ void __launch_bounds__(THREADS, 1)
+    scatter_staged_kernel(const Tile *__restrict__ tiles, const long long *__restrict__ n_tiles_p,
+                          long long capacity, const PairInfo *__restrict__ pairs, int td,
+                          int stage_bytes, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    unsigned char *stages = smem + 128;
+    unsigned char *direct = stages + (size_t)S * (size_t)stage_bytes;
+    long long n = *n_tiles_p;
+    if (n > capacity)
+        n = capacity;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < S; ++k)
+            mbar_init(smem_addr(&bars[k]), 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const long long G = gridDim.x;
+    if (warp == 0)
+        for (int k = 0; k < S; ++k)
+            issue_stage(tiles, blockIdx.x + k * G, n, stages + (size_t)k * stage_bytes,
+                        smem_addr(&bars[k]), stage_bytes);
+    uint32_t phase = 0;
+    int st = 0;
+    for (long long ti = blockIdx.x; ti < n; ti += G) {
+        const Tile t = tiles[ti];
+        unsigned char *stage = stages + (size_t)st * stage_bytes;
+        const uint32_t bar = smem_addr(&bars[st]);
+        if ((PATHS & PATH_COPY) && tma_eligible(t, stage_bytes)) {
+            const bool ok = mbar_wait_bounded(bar, (phase >> st) & 1u, STAGE_WAIT_LIMIT_NS);
+            if (!__syncthreads_and(ok)) {
+                if (threadIdx.x == 0) {
+                    atomicExch(status, 1);
+                    for (int k = 0; k < S; ++k)
+                        mbar_wait_bounded(smem_addr(&bars[k]), (phase >> k) & 1u,
+                                          STAGE_WAIT_LIMIT_NS / 4);
+                }
+                __syncthreads();
+                return;
+            }
+            phase ^= 1u << st;
+            consume_stage<THREADS, U>(t, stage);
+        } else if ((PATHS & PATH_COPY) && !(t.kind & (KIND_TRANS | KIND_SCALED))) {
+            copy_tile<THREADS, U>(t);
+        } else if ((PATHS & PATH_TRANSPOSE) && (t.kind & KIND_TRANS) &&
+                   !(t.kind & KIND_SCALED)) {
+            transpose_dispatch<THREADS>(t, direct, td);
+        } else if (PATHS & PATH_SCALED) {
+            scaled_dispatch<THREADS>(t, pairs, direct, td);
+        }
+        __syncthreads(); // the stage is free again
+        if (warp == 0)
+            issue_stage(tiles, ti + (long long)S * G, n, stage, bar, stage_bytes);
+        st = (st + 1 == S) ? 0 : st + 1;
+    }
+}
+
+template <typename K>
+cudaError_t launch_kernel(K k, const PlanDevice &d, const ScatterConfig &cfg, size_t smem,
+                          cudaStream_t s, bool staged) {
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)
             return e;
     }
-    k<<<cfg.grid, THREADS, cfg.smem_bytes, s>>>(d.tiles, d.n_tiles, d.tile_capacity, d.pairs,
-                                                cfg.tile_dim);
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, cfg.threads, smem);
+    if (e != cudaSuccess)
+        return e;
+    if (occ < 1)
+        return cudaErrorInvalidConfiguration;
+    // a persistent grid must be resident at once (static striding)
+    long long grid = cfg.grid;
+    const long long resident = (long long)cfg.sm_count * occ;
+    if (cfg.sm_count > 0 && grid > resident)
+        grid = resident;
+    if (grid < 1)
+        grid = 1;
+    if (staged)
+        ((void (*)(const Tile *, const long long *, long long, const PairInfo *, int, int,
+                   int *))k)<<<(unsigned)grid, cfg.threads, smem, s>>>(
+            d.tiles, d.n_tiles, d.tile_capacity, d.pairs, cfg.tile_dim, cfg.stage_bytes,
+            d.status);
+    else
+        ((void (*)(const Tile *, const long long *, long long, const PairInfo *,
+                   int))k)<<<(unsigned)grid, cfg.threads, smem, s>>>(
+            d.tiles, d.n_tiles, d.tile_capacity, d.pairs, cfg.tile_dim);
     return cudaGetLastError();
+}
+
+template <int THREADS, int U, int PATHS>
+cudaError_t launch_t(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+    if ((PATHS & PATH_COPY) && cfg.stages >= 2) {
+        const size_t smem = staged_smem_bytes(cfg);
+        switch (cfg.stages) {
+        case 2: return launch_kernel(scatter_staged_kernel<THREADS, U, PATHS, 2>, d, cfg, smem, s, true);
+        case 3: return launch_kernel(scatter_staged_kernel<THREADS, U, PATHS, 3>, d, cfg, smem, s, true);
+        default: return launch_kernel(scatter_staged_kernel<THREADS, U, PATHS, 4>, d, cfg, smem, s, true);
+        }
+    }
+    return launch_kernel(scatter_kernel<THREADS, U, PATHS>, d, cfg, cfg.smem_bytes, s, false);
 }
 
 template <int THREADS, int PATHS>
@@ -535,7 +850,6 @@ cudaError_t launch_u(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t
     switch (cfg.unroll) {
     case 1: return launch_t<THREADS, 1, PATHS>(d, cfg, s);
     case 2: return launch_t<THREADS, 2, PATHS>(d, cfg, s);
-    case 8: return launch_t<THREADS, 8, PATHS>(d, cfg, s);
     default: return launch_t<THREADS, 4, PATHS>(d, cfg, s);
     }
 }
@@ -557,12 +871,20 @@ size_t transpose_smem_bytes(int tile_dim, int esz) {
     return (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;
 }
 
+int stage_bytes_for(int tile_bytes) {
+    const long long b = (long long)tile_bytes * 9 / 8 + 512;
+    return (int)((b + 127) / 128 * 128);
+}
+
+size_t staged_smem_bytes(const ScatterConfig &cfg) {
+    return 128 + (size_t)cfg.stages * (size_t)cfg.stage_bytes + cfg.trans_bytes;
+}
+
 cudaError_t launch_scatter(const PlanDevice &d, const ScatterConfig &cfg,
                            cudaStream_t stream) {
     if (cfg.grid <= 0)
         return cudaErrorInvalidConfiguration;
     switch (cfg.threads) {
-    case 128: return launch_p<128>(d, cfg, stream);
     case 512: return launch_p<512>(d, cfg, stream);
     default: return launch_p<256>(d, cfg, stream);
     }

@@ -125,7 +125,10 @@ typedef struct g2g_tuning {
     int32_t ctas_per_sm;      /* persistent grid = ctas_per_sm x SM count   */
     int32_t threads;          /* threads per CTA: 128, 256 or 512           */
     int32_t unroll;           /* 16-byte chunks in flight per thread: 1,2,4,8 */
-    int32_t reserved[3];
+    int32_t stages;           /* plain copies: -1 = loads through registers,
+                                 2..4 = TMA bulk copies into a ring of that
+                                 many shared-memory stages (0 = default)    */
+    int32_t reserved[2];
 } g2g_tuning;
 
 typedef struct g2g_plan_info {
@@ -137,7 +140,9 @@ typedef struct g2g_plan_info {
     int64_t bytes_min_traffic;/* 2x bytes_moved (3x for pieces with beta!=0) */
     int64_t metadata_bytes;   /* device memory held by the plan              */
     int32_t graph_captured;   /* 1 after g2g_plan_capture_graph              */
-    int32_t reserved;
+    int32_t device_status;    /* 0, or the error a kernel of the plan raised
+                                 (1 = a bounded wait expired); reading it
+                                 synchronises with the plan's last execution */
     g2g_tuning tuning;        /* knobs in effect                             */
 } g2g_plan_info;
 
