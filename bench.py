@@ -356,6 +356,14 @@ def run_ours(args):
         e2e = run_e2e(lib, w, dev_i, dev_f, args.e2e_steps, stream, ws)
     capi.check(lib.g2g_plan_destroy(plan))
 
+    batched = serving = None
+    if args.batch and rank == 0:
+        batched, pool = run_batched(lib, dev, stream, 20, peak)
+        if args.serving:
+            serving = run_serving(lib, pool, [1000, 5000, 20000], 1.0)
+        del pool
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and ws == 1 and args.cpu_reps > 0:
         host_i = [t.cpu().numpy() for t in dev_i]
@@ -375,6 +383,7 @@ def run_ours(args):
             "data": "synthetic (seeded random bit patterns, device-resident)",
             "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
+            "batched_stream": batched, "serving": serving,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
                      "tuning": {k: getattr(info.tuning, k) for k in
@@ -386,6 +395,161 @@ def run_ours(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def _device_arenas(w, dev, seed):
+    import torch
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    di = [torch.randint(0, 256, (L.arena_bytes,), dtype=torch.uint8, device=dev,
+                        generator=gen) for L in w.inits]
+    df = [torch.randint(0, 256, (L.arena_bytes,), dtype=torch.uint8, device=dev,
+                        generator=gen) for L in w.finals]
+    return di, df
+
+
+def _desc_array(layouts, tensors, keep):
+    from grid2grid_gb300 import capi
+    arr = (capi.LayoutDesc * len(layouts))()
+    for k, (L, t) in enumerate(zip(layouts, tensors)):
+        d, kk = L.desc(t.data_ptr())
+        arr[k] = d
+        keep.append(kk)
+    return arr
+
+
+def _time_steps(stream, fn, steps, warmup):
+    import torch
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            fn()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+    stream.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def run_batched(lib, dev, stream, steps, peak):
+    """uneven_batch_256: 256 redistributions of uneven shapes and dtypes.
+    batched = one plan over all pairs (the vector transform), autotuned and
+    replayed as a captured CUDA graph: ONE launch per step. plain = the same
+    256 transforms with cached per-transform plans, one launch each.
+    multi_plan = those 256 cached plans issued as one launch."""
+    from grid2grid_gb300 import capi
+    from grid2grid_gb300 import workloads as W
+    w = W.uneven_batch(256)
+    di, df = _device_arenas(w, dev, 77)
+    keep = []
+    n = len(w.inits)
+    dI, dF = _desc_array(w.inits, di, keep), _desc_array(w.finals, df, keep)
+    dts = (C.c_int * n)(*w.dtypes())
+    sp = C.c_void_p(stream.cuda_stream)
+    plan = C.c_void_p()
+    t0 = time.perf_counter()
+    capi.check(lib.g2g_plan_create_batch(n, dI, dF, dts, None, sp, C.byref(plan)))
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    tuned = capi.Tuning()
+    capi.check(lib.g2g_plan_autotune(plan, sp, 2, C.byref(tuned)))
+    capi.check(lib.g2g_plan_capture_graph(plan, sp))
+    info = capi.PlanInfo()
+    capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
+    ms_b = _time_steps(stream, lambda: capi.check(lib.g2g_plan_execute(plan, sp)),
+                       steps, 3)
+    plans = (C.c_void_p * n)()
+    t0 = time.perf_counter()
+    for k in range(n):
+        p = C.c_void_p()
+        capi.check(lib.g2g_plan_create(C.byref(dI[k]), C.byref(dF[k]), dts[k], None, sp,
+                                       C.byref(p)))
+        plans[k] = p.value
+    plans_ms = (time.perf_counter() - t0) * 1e3
+
+    def plain():
+        for k in range(n):
+            capi.check(lib.g2g_plan_execute(plans[k], sp))
+    ms_p = _time_steps(stream, plain, max(2, steps // 4), 1)
+    ms_m = _time_steps(stream, lambda: capi.check(lib.g2g_plans_execute(n, plans, sp)),
+                       steps, 2)
+    for k in range(n):
+        capi.check(lib.g2g_plan_destroy(plans[k]))
+    capi.check(lib.g2g_plan_destroy(plan))
+    b = w.bytes_moved
+    return {
+        "workload": w.name, "bytes_per_step": b, "pieces": info.n_pieces,
+        "tiles": info.n_tiles,
+        "batched": {"value": round(b / (ms_b * 1e-3) / 1e9, 2), "unit": UNIT,
+                    "ms_per_step": round(ms_b, 4), "launches_per_step": 1,
+                    "roofline_frac": round(info.bytes_min_traffic / (ms_b * 1e-3) / 1e9 / peak, 4),
+                    "plan_ms": round(plan_ms, 1),
+                    "tuning": {k: getattr(tuned, k) for k in
+                               ("tile_bytes", "tile_dim", "ctas_per_sm", "threads", "unroll",
+                                "stages")},
+                    "graph": True},
+        "plain_launches": {"value": round(b / (ms_p * 1e-3) / 1e9, 2), "unit": UNIT,
+                           "ms_per_step": round(ms_p, 4), "launches_per_step": n,
+                           "plan_ms_total": round(plans_ms, 1)},
+        "multi_plan_launch": {"value": round(b / (ms_m * 1e-3) / 1e9, 2), "unit": UNIT,
+                              "ms_per_step": round(ms_m, 4), "launches_per_step": 1},
+        "speedup_batched_vs_plain": round(ms_p / ms_b, 3),
+    }, (w, di, df, dI, dF, dts, keep)
+
+
+def run_serving(lib, pool, rates, duration_s, seed=5):
+    """Open-loop Poisson arrivals of requests drawn from the uneven batch
+    pool (plans cached), through the continuous-batching server and through
+    plain per-request launches (max_batch_requests = 1, one launch in
+    flight). Latency = completion - arrival."""
+    from grid2grid_gb300 import capi
+    w, di, df, dI, dF, dts, keep = pool
+    n = len(w.inits)
+    rng = np.random.default_rng(seed)
+    servers = {}
+    for mode, cfg in (("continuous", dict(max_batch_requests=256, max_launches_in_flight=3)),
+                      ("plain", dict(max_batch_requests=1, max_launches_in_flight=1))):
+        c = capi.ServerConfig()
+        c.hbm_budget_bytes = 120 * 10**9
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        srv = C.c_void_p()
+        capi.check(lib.g2g_server_create(C.byref(c), C.byref(srv)))
+        servers[mode] = srv
+    out = {"budget_bytes": 120 * 10**9, "duration_s": duration_s, "rates": {}}
+    try:
+        for mode, srv in servers.items():  # warm the plan caches
+            idx = (C.c_int32 * n)(*range(n))
+            arr = (C.c_double * n)(*([0.0] * n))
+            times = (capi.RequestTimes * n)()
+            capi.check(lib.g2g_server_replay(srv, n, dI, dF, dts, None, n, idx, arr, times))
+        for rate in rates:
+            N = int(rate * duration_s)
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=N))
+            pick = rng.integers(0, n, size=N).astype(np.int32)
+            res = {}
+            for mode, srv in servers.items():
+                idx = pick.ctypes.data_as(C.POINTER(C.c_int32))
+                arr = arrivals.astype(np.float64)
+                times = (capi.RequestTimes * N)()
+                capi.check(lib.g2g_server_replay(srv, n, dI, dF, dts, None, N, idx,
+                                                 arr.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 times))
+                t = np.ctypeslib.as_array(times)
+                lat = (t["complete_ns"] - t["submit_ns"]) / 1e3
+                span = (t["complete_ns"].max() - t["submit_ns"].min()) / 1e9
+                res[mode] = {"p50_us": round(float(np.percentile(lat, 50)), 1),
+                             "p99_us": round(float(np.percentile(lat, 99)), 1),
+                             "mean_us": round(float(lat.mean()), 1),
+                             "GBps": round(float(t["bytes"].sum()) / span / 1e9, 2),
+                             "mean_batch": round(float(t["batch_size"].mean()), 2),
+                             "requests": N}
+            out["rates"][str(rate)] = res
+    finally:
+        for srv in servers.values():
+            capi.check(lib.g2g_server_destroy(srv))
+    return out
 
 
 def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
@@ -448,6 +612,10 @@ def main(argv=None):
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-reps", type=int, default=2)
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-batch", dest="batch", action="store_false",
+                    help="skip the 256-transform batched stream")
+    ap.add_argument("--no-serving", dest="serving", action="store_false",
+                    help="skip the Poisson serving measurement")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

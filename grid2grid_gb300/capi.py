@@ -82,6 +82,39 @@ class Tuning(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("hbm_budget_bytes", C.c_int64),
+        ("max_launches_in_flight", C.c_int32),
+        ("max_batch_requests", C.c_int32),
+        ("plan_cache_entries", C.c_int32),
+        ("reserved", C.c_int32 * 3),
+    ]
+
+
+class RequestTimes(C.Structure):
+    _fields_ = [
+        ("submit_ns", C.c_int64),
+        ("launch_ns", C.c_int64),
+        ("complete_ns", C.c_int64),
+        ("bytes", C.c_int64),
+        ("status", C.c_int32),
+        ("batch_size", C.c_int32),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64),
+        ("completed", C.c_int64),
+        ("launches", C.c_int64),
+        ("plan_cache_hits", C.c_int64),
+        ("plan_cache_misses", C.c_int64),
+        ("bytes_completed", C.c_int64),
+        ("inflight_bytes_peak", C.c_int64),
+    ]
+
+
 class PlanInfo(C.Structure):
     _fields_ = [
         ("n_pairs", C.c_int32),
@@ -120,6 +153,7 @@ SIGNATURES = [
      [C.c_int32, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.POINTER(C.c_int),
       C.POINTER(Op), _VP, C.POINTER(_VP)]),
     ("g2g_plan_execute", C.c_int, [_VP, _VP]),
+    ("g2g_plans_execute", C.c_int, [C.c_int32, C.POINTER(_VP), _VP]),
     ("g2g_plan_capture_graph", C.c_int, [_VP, _VP]),
     ("g2g_plan_set_tuning", C.c_int, [_VP, C.POINTER(Tuning)]),
     ("g2g_plan_autotune", C.c_int, [_VP, _VP, C.c_int32, C.POINTER(Tuning)]),
@@ -132,6 +166,16 @@ SIGNATURES = [
       C.POINTER(Op), _VP]),
     ("g2g_grid_cover", C.c_int,
      [_I32P, C.c_int32, _I32P, C.c_int32, _I32P, _I32P, _VP]),
+    ("g2g_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(_VP)]),
+    ("g2g_server_submit", C.c_int,
+     [_VP, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op),
+      C.POINTER(C.c_uint64)]),
+    ("g2g_server_wait", C.c_int, [_VP, C.c_uint64, C.c_int64, C.POINTER(RequestTimes)]),
+    ("g2g_server_replay", C.c_int,
+     [_VP, C.c_int32, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.POINTER(C.c_int),
+      C.POINTER(Op), C.c_int64, _I32P, C.POINTER(C.c_double), C.POINTER(RequestTimes)]),
+    ("g2g_server_get_stats", C.c_int, [_VP, C.POINTER(ServerStats)]),
+    ("g2g_server_destroy", C.c_int, [_VP]),
 ]
 
 _lib = None

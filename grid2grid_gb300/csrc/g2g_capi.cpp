@@ -8,6 +8,7 @@
 // block is not held by its owner -- into G2G_ERROR_INVALID_ARGUMENT with a
 // message, before any device work is queued.
 #include "../../include/grid2grid_gb300.h"
+#include "g2g_host.hpp"
 #include "g2g_internal.hpp"
 #include "g2g_launch.hpp"
 
@@ -24,9 +25,10 @@
 #include <vector>
 
 namespace {
-
 thread_local std::string t_last_error;
+}
 
+namespace g2g {
 g2g_status fail(g2g_status st, const char *fmt, ...) {
     char buf[1024];
     va_list ap;
@@ -36,6 +38,10 @@ g2g_status fail(g2g_status st, const char *fmt, ...) {
     t_last_error = buf;
     return st;
 }
+} // namespace g2g
+
+namespace {
+using g2g::fail;
 
 #define G2G_CUDA(call)                                                                  \
     do {                                                                                \
@@ -283,12 +289,12 @@ struct PairHost {
 g2g_tuning default_tuning() {
     g2g_tuning t;
     std::memset(&t, 0, sizeof(t));
-    t.tile_bytes = 64 * 1024;
+    t.tile_bytes = 16 * 1024;
     t.tile_dim = 32;
-    t.ctas_per_sm = 4;
+    t.ctas_per_sm = 8;
     t.threads = 256;
-    t.unroll = 2;
-    t.stages = 3;
+    t.unroll = 4;
+    t.stages = -1; // TMA staging is opt-in (no faster on measured workloads)
     return t;
 }
 
@@ -346,13 +352,18 @@ struct g2g_plan {
     void *dmem = nullptr;
     size_t dmem_bytes = 0;
     g2g::PlanDevice dev;
-    long long n_tiles = 0;
+    long long n_tiles = 0; // copy tiles + CTA-level tiles
+    long long n_copy = 0;
     long long n_pieces = 0;
     cudaStream_t last_stream = nullptr;
     cudaEvent_t done = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
 };
+
+namespace g2g {
+int64_t plan_bytes_moved(const g2g_plan *plan) { return plan ? plan->bytes_moved : 0; }
+} // namespace g2g
 
 namespace {
 
@@ -555,6 +566,7 @@ g2g_status plan_on_device(g2g_plan &pl) {
     const size_t upload_end = off;
     const size_t o_parts = take(sizeof(g2g::Part) * (size_t)pl.n_parts);
     const size_t o_cells = take(sizeof(long long) * (size_t)pl.n_cells);
+    const size_t o_cells_cta = take(sizeof(long long) * (size_t)pl.n_cells);
     const size_t o_sums = take(sizeof(long long) * (size_t)g2g::scan_sums_capacity(pl.n_cells));
     const size_t o_counters = take(64);
     const size_t o_tiles = take(sizeof(g2g::Tile) * (size_t)capacity);
@@ -577,11 +589,13 @@ g2g_status plan_on_device(g2g_plan &pl) {
     d.dst_tables = (g2g::DstEntry *)(base + o_dst);
     d.parts = (g2g::Part *)(base + o_parts);
     d.cell_tiles = (long long *)(base + o_cells);
+    d.cell_tiles_cta = (long long *)(base + o_cells_cta);
     d.scan_sums = (long long *)(base + o_sums);
-    d.n_tiles = (long long *)(base + o_counters);
+    d.n_copy = (long long *)(base + o_counters);
     d.n_pieces = (unsigned long long *)(base + o_counters + 8);
     d.overflow = (int *)(base + o_counters + 16);
     d.status = (int *)(base + o_counters + 24);
+    d.n_cta = (long long *)(base + o_counters + 32);
     d.tiles = (g2g::Tile *)(base + o_tiles);
     d.tile_capacity = capacity;
     d.max_cells_per_pair = pl.max_cells_per_pair;
@@ -617,20 +631,21 @@ g2g_status plan_on_device(g2g_plan &pl) {
         e = cudaMemsetAsync(base + o_counters, 0, 64, ds->plan_stream);
     if (e == cudaSuccess)
         e = g2g::launch_plan(d, pl.n_pairs, 0, pl.n_cells, ds->plan_stream);
-    long long counters[3] = {0, 0, 0};
+    long long counters[5] = {0, 0, 0, 0, 0};
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(pinned, base + o_counters, 24, cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(pinned, base + o_counters, 40, cudaMemcpyDeviceToHost,
                             ds->plan_stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(ds->plan_stream);
     if (e == cudaSuccess)
-        std::memcpy(counters, pinned, 24);
+        std::memcpy(counters, pinned, 40);
     G2G_CUDA(e);
     if (((int *)counters)[4] != 0)
         return fail(G2G_ERROR_CUDA,
                     "internal error: tile work list exceeded its bound (%lld > %lld)",
-                    counters[0], (long long)capacity);
-    pl.n_tiles = counters[0];
+                    counters[0] + counters[4], (long long)capacity);
+    pl.n_copy = counters[0];
+    pl.n_tiles = counters[0] + counters[4];
     pl.n_pieces = counters[1];
     return G2G_SUCCESS;
 }
@@ -661,6 +676,50 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
             --st;
         c.stages = st >= 2 ? st : 0;
     }
+    return c;
+}
+
+void add_to_list(g2g::PlanList &l, const g2g_plan &pl) {
+    g2g::PlanRef &r = l.p[l.n++];
+    r.tiles = pl.dev.tiles;
+    r.pairs = pl.dev.pairs;
+    r.first_copy = l.total_copy;
+    r.first_cta = l.total_cta;
+    r.n_copy = pl.n_copy;
+    l.total_copy += pl.n_copy;
+    l.total_cta += pl.n_tiles - pl.n_copy;
+}
+
+g2g::PlanList single_list(const g2g_plan &pl) {
+    g2g::PlanList l;
+    l.status = pl.dev.status;
+    add_to_list(l, pl);
+    return l;
+}
+
+// Configuration that covers every plan of a multi-plan launch: the union of
+// their tile paths, the largest shared-memory need, the first plan's knobs.
+g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
+    g2g::ScatterConfig c = scatter_config(*plans[0]);
+    long long tiles = 0;
+    for (int k = 0; k < n; ++k) {
+        const g2g::ScatterConfig ck = scatter_config(*plans[k]);
+        c.paths |= ck.paths;
+        c.trans_bytes = std::max(c.trans_bytes, ck.trans_bytes);
+        c.smem_bytes = std::max(c.smem_bytes, ck.smem_bytes);
+        tiles += plans[k]->n_tiles;
+    }
+    if (c.stages >= 2) {
+        while (c.stages >= 2 &&
+               128 + (size_t)c.stages * c.stage_bytes + c.trans_bytes > kMaxSmemPerCta)
+            --c.stages;
+        if (c.stages < 2)
+            c.stages = 0;
+    } else if (c.paths & 1) {
+        c.stages = 0;
+    }
+    long long g = (long long)c.sm_count * plans[0]->tuning.ctas_per_sm;
+    c.grid = (int)std::max<long long>(1, std::min(g, std::max<long long>(tiles, 1)));
     return c;
 }
 
@@ -699,14 +758,7 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
         return st;
     }
     G2G_CUDA(cudaEventCreateWithFlags(&pl->done, cudaEventDisableTiming));
-    // Large tiles keep enough bytes in flight with fewer, deeper threads;
-    // small tiles (many small pieces) want more resident CTAs instead
-    // (measured on GB300 for 8 KB and ~27 KB average tiles).
-    if (pl->n_tiles > 0 && pl->bytes_moved / pl->n_tiles >= 24 * 1024 && pl->paths == 1) {
-        pl->tuning.unroll = 4;
-        pl->tuning.ctas_per_sm = 8;
-    }
-    (void)0;
+
     *out = pl;
     return G2G_SUCCESS;
 }
@@ -744,11 +796,43 @@ g2g_status g2g_plan_execute(g2g_plan *plan, void *stream) {
         if (plan->graph && plan->graph_stream == s) {
             G2G_CUDA(cudaGraphLaunch(plan->graph, s));
         } else {
-            G2G_CUDA(g2g::launch_scatter(plan->dev, scatter_config(*plan), s));
+            G2G_CUDA(g2g::launch_scatter(single_list(*plan), scatter_config(*plan), s));
         }
     }
     G2G_CUDA(cudaEventRecord(plan->done, s));
     plan->last_stream = s;
+    return G2G_SUCCESS;
+}
+
+g2g_status g2g_plans_execute(int32_t n_plans, g2g_plan *const *plans, void *stream) {
+    if (n_plans < 1 || !plans)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "no plans to execute");
+    for (int k = 0; k < n_plans; ++k) {
+        if (!plans[k])
+            return fail(G2G_ERROR_INVALID_ARGUMENT, "plan %d is NULL", k);
+        if (plans[k]->device != plans[0]->device)
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "plans of one launch must live on one device (plan %d)", k);
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    G2G_CUDA(cudaSetDevice(plans[0]->device));
+    for (int base = 0; base < n_plans; base += g2g::kMaxPlansPerLaunch) {
+        const int n = std::min(n_plans - base, g2g::kMaxPlansPerLaunch);
+        g2g::PlanList l;
+        l.n = 0;
+        l.status = plans[base]->dev.status;
+        for (int k = 0; k < n; ++k) {
+            const g2g_plan *p = plans[base + k];
+            if (p->n_tiles > 0)
+                add_to_list(l, *p);
+        }
+        if (l.n > 0)
+            G2G_CUDA(g2g::launch_scatter(l, merged_config(plans + base, n), s));
+    }
+    for (int k = 0; k < n_plans; ++k) {
+        G2G_CUDA(cudaEventRecord(plans[k]->done, s));
+        plans[k]->last_stream = s;
+    }
     return G2G_SUCCESS;
 }
 
@@ -768,7 +852,7 @@ g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream) {
         return G2G_SUCCESS;
     cudaGraph_t g = nullptr;
     G2G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t le = g2g::launch_scatter(plan->dev, scatter_config(*plan), s);
+    cudaError_t le = g2g::launch_scatter(single_list(*plan), scatter_config(*plan), s);
     cudaError_t ee = cudaStreamEndCapture(s, &g);
     G2G_CUDA(le);
     G2G_CUDA(ee);

@@ -14,10 +14,12 @@ struct PlanDevice {
     SrcEntry *src_tables = nullptr;
     DstEntry *dst_tables = nullptr;
     Part *parts = nullptr;
-    long long *cell_tiles = nullptr;   // counts, then exclusive offsets
+    long long *cell_tiles = nullptr;     // copy-tile counts, then exclusive offsets
+    long long *cell_tiles_cta = nullptr; // transposed/scaled tile counts, then offsets
     long long *scan_sums = nullptr;
-    Tile *tiles = nullptr;
-    long long *n_tiles = nullptr;      // device scalar: tiles in the work list
+    Tile *tiles = nullptr;               // [copy tiles | CTA-level tiles]
+    long long *n_copy = nullptr;         // device scalar: copy tiles
+    long long *n_cta = nullptr;          // device scalar: CTA-level tiles
     unsigned long long *n_pieces = nullptr;
     int *overflow = nullptr;           // device flag: tile capacity exceeded
     int *status = nullptr;             // device flag: kernel error (bounded wait expired)
@@ -33,6 +35,26 @@ long long scan_sums_capacity(long long n_cells);
 // Grid cover (interval_cover form) of split vector a by b, device arrays.
 cudaError_t launch_cover(const int32_t *a, int na, const int32_t *b, int nb,
                          int32_t *start, int32_t *end, cudaStream_t stream);
+
+// Plans executed by one launch of the gather-scatter: a persistent kernel
+// walks the concatenation of their work lists. Passed by value as a
+// __grid_constant__ kernel parameter (8 KB), so a launch uploads nothing.
+constexpr int kMaxPlansPerLaunch = 256;
+struct PlanRef {
+    const Tile *tiles;       // the plan's work list: n_copy copy tiles, then n_cta
+    const PairInfo *pairs;
+    long long first_copy;    // index of the plan's first copy tile in the launch
+    long long first_cta;     // index of the plan's first CTA-level tile
+    long long n_copy;
+};
+struct PlanList {
+    int n = 0;
+    int pad = 0;
+    long long total_copy = 0; // copy tiles over all plans (warp-level items)
+    long long total_cta = 0;  // transposed / scaled tiles (CTA-level items)
+    int *status = nullptr;
+    PlanRef p[kMaxPlansPerLaunch];
+};
 
 struct ScatterConfig {
     int threads = 256;       // 128, 256 or 512
@@ -59,8 +81,8 @@ size_t staged_smem_bytes(const ScatterConfig &cfg);
 // bytes needs.
 size_t transpose_smem_bytes(int tile_dim, int esz);
 
-// Launches the gather-scatter over d.tiles[0, *d.n_tiles).
-cudaError_t launch_scatter(const PlanDevice &d, const ScatterConfig &cfg,
+// Launches the gather-scatter over the plans of `list`.
+cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,
                            cudaStream_t stream);
 
 } // namespace g2g

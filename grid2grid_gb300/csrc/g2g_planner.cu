@@ -15,8 +15,10 @@
 //     the number of tiles the piece is cut into. Cells are numbered column
 //     part by column part (row parts fastest), which fixes the order of the
 //     work list.
-//  3. scan_*               exclusive scan of the tile counts over all cells of
-//     all pairs (three-phase: per-CTA sums, scan of sums, apply).
+//  3. scan_*               exclusive scans of the tile counts over all cells of
+//     all pairs (three-phase: per-CTA sums, scan of sums, apply), one for
+//     plain-copy cells and one for transposed / scaled cells: the work list
+//     holds every copy tile (warp-level work) before the CTA-level tiles.
 //  4. emit_tiles_kernel    one warp per cell writes the cell's tiles, with the
 //     source address computed as block<T>::subblock does (block.cpp:165-196)
 //     and the destination address in the final owner's block.
@@ -107,10 +109,17 @@ __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
     }
 }
 
+// Plain copies are warp-level work items, transposed and scaled tiles
+// CTA-level ones; the work list holds all copy tiles first.
+__device__ inline bool is_copy_kind(uint32_t kind) {
+    return !(kind & (KIND_TRANS | KIND_SCALED));
+}
+
 __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pairs,
                                   const Part *__restrict__ parts,
                                   const SrcEntry *__restrict__ src_tables,
                                   long long *__restrict__ cell_tiles,
+                                  long long *__restrict__ cell_tiles_cta,
                                   unsigned long long *__restrict__ n_pieces) {
     const int pi = blockIdx.y;
     const PairInfo p = pairs[pi];
@@ -128,6 +137,7 @@ __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pair
         Part pr = parts[p.row_parts + u];
         Part pc = parts[p.col_parts + v];
         long long cnt = 0;
+        bool copy = true;
         if (pr.len > 0 && pc.len > 0) {
             const SrcEntry e = src_tables[p.src_table + (long long)pr.ia * p.a_nc + pc.ia];
             uint32_t kind = p.kind | ((e.flags & 1u) ? KIND_TRANS : 0u) |
@@ -135,9 +145,11 @@ __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pair
             int tr, tc;
             tile_shape(p, kind, pr.len, pc.len, tr, tc);
             cnt = (long long)((pr.len + tr - 1) / tr) * ((pc.len + tc - 1) / tc);
+            copy = is_copy_kind(kind);
             ++local_pieces;
         }
-        cell_tiles[p.cells + cidx] = cnt;
+        cell_tiles[p.cells + cidx] = copy ? cnt : 0;
+        cell_tiles_cta[p.cells + cidx] = copy ? 0 : cnt;
     }
     // one atomic per warp
     for (int off = 16; off > 0; off >>= 1)
@@ -237,6 +249,8 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
                                   const SrcEntry *__restrict__ src_tables,
                                   const DstEntry *__restrict__ dst_tables,
                                   const long long *__restrict__ cell_offsets,
+                                  const long long *__restrict__ cell_offsets_cta,
+                                  const long long *__restrict__ n_copy,
                                   Tile *__restrict__ tiles, long long capacity,
                                   int *__restrict__ overflow) {
     const int pi = blockIdx.y;
@@ -264,7 +278,9 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
         const int ntr = (pr.len + tr - 1) / tr;
         const int ntc = (pc.len + tc - 1) / tc;
         const long long ntiles = (long long)ntr * ntc;
-        const long long base = cell_offsets[p.cells + cidx];
+        const long long base = is_copy_kind(kind)
+                                   ? cell_offsets[p.cells + cidx]
+                                   : *n_copy + cell_offsets_cta[p.cells + cidx];
         if (base + ntiles > capacity) {
             if (lane == 0)
                 atomicExch(overflow, 1);
@@ -327,10 +343,10 @@ cudaError_t launch_plan(const PlanDevice &d, int n_pairs, int max_nrp_ncp_thread
         gx = 1;
     cell_tiles_kernel<<<dim3(gx, n_pairs), 256, 0, stream>>>(d.pairs, n_pairs, d.parts,
                                                              d.src_tables, d.cell_tiles,
-                                                             d.n_pieces);
+                                                             d.cell_tiles_cta, d.n_pieces);
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
-    // exclusive scan of cell_tiles -> tile offsets, total -> *n_tiles
+    // exclusive scans of both count arrays -> tile offsets; totals -> n_copy, n_cta
     long long chunk = 4096;
     long long nblk = (n_cells + chunk - 1) / chunk;
     if (nblk > SCAN_THREADS * 64) {
@@ -339,11 +355,15 @@ cudaError_t launch_plan(const PlanDevice &d, int n_pairs, int max_nrp_ncp_thread
     }
     if (nblk < 1)
         nblk = 1;
-    scan_partial_kernel<<<(unsigned)nblk, 256, 0, stream>>>(d.cell_tiles, n_cells, chunk,
-                                                           d.scan_sums);
-    scan_sums_kernel<<<1, SCAN_THREADS, 0, stream>>>(d.scan_sums, (int)nblk, d.n_tiles);
-    scan_apply_kernel<<<(unsigned)nblk, 256, 0, stream>>>(d.cell_tiles, n_cells, chunk,
-                                                         d.scan_sums);
+    long long *arrays[2] = {d.cell_tiles, d.cell_tiles_cta};
+    long long *totals[2] = {d.n_copy, d.n_cta};
+    for (int k = 0; k < 2; ++k) {
+        scan_partial_kernel<<<(unsigned)nblk, 256, 0, stream>>>(arrays[k], n_cells, chunk,
+                                                               d.scan_sums);
+        scan_sums_kernel<<<1, SCAN_THREADS, 0, stream>>>(d.scan_sums, (int)nblk, totals[k]);
+        scan_apply_kernel<<<(unsigned)nblk, 256, 0, stream>>>(arrays[k], n_cells, chunk,
+                                                             d.scan_sums);
+    }
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;
     int ex = (int)((d.max_cells_per_pair + 7) / 8);
@@ -352,8 +372,8 @@ cudaError_t launch_plan(const PlanDevice &d, int n_pairs, int max_nrp_ncp_thread
     if (ex < 1)
         ex = 1;
     emit_tiles_kernel<<<dim3(ex, n_pairs), 256, 0, stream>>>(
-        d.pairs, d.splits, d.parts, d.src_tables, d.dst_tables, d.cell_tiles, d.tiles,
-        d.tile_capacity, d.overflow);
+        d.pairs, d.splits, d.parts, d.src_tables, d.dst_tables, d.cell_tiles,
+        d.cell_tiles_cta, d.n_copy, d.tiles, d.tile_capacity, d.overflow);
     return cudaGetLastError();
 }
 

@@ -118,11 +118,9 @@ __device__ __forceinline__ uint4 funnel_words(uint4 lo, uint4 hi, uint32_t q) {
 // aligned destination chunk. Only 16-byte blocks overlapping the column are
 // read, so no access leaves the pages the column lives in; stores cover
 // exactly the column (word-masked head and tail chunks).
-template <int THREADS, int U>
-__device__ __forceinline__ void copy_tile(const Tile &t) {
-    constexpr int NWARP = THREADS / 32;
+template <int NWARP, int U>
+__device__ __forceinline__ void copy_tile(const Tile &t, const int warp) {
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
     const int esz = kind_esz(t.kind);
     const int L = t.rows * esz; // bytes per column, <= 4096
     if (L <= 0 || t.cols <= 0)
@@ -207,6 +205,32 @@ __device__ __forceinline__ void copy_tile(const Tile &t) {
             }
         }
     }
+}
+
+// Copy tile `ti` (warp-level items) / CTA-level tile `ti` of the plans of a
+// launch, and the pair table of its plan.
+__device__ __forceinline__ int plan_of(const PlanList &L, long long ti, bool copy) {
+    int lo = 0, hi = L.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((copy ? L.p[mid].first_copy : L.p[mid].first_cta) <= ti)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ const Tile *locate_copy(const PlanList &L, long long ti,
+                                                   const PairInfo *&pairs) {
+    const int k = plan_of(L, ti, true);
+    pairs = L.p[k].pairs;
+    return L.p[k].tiles + (ti - L.p[k].first_copy);
+}
+__device__ __forceinline__ const Tile *locate_cta(const PlanList &L, long long ti,
+                                                  const PairInfo *&pairs) {
+    const int k = plan_of(L, ti, false);
+    pairs = L.p[k].pairs;
+    return L.p[k].tiles + L.p[k].n_copy + (ti - L.p[k].first_cta);
 }
 
 // ------------------------------------------------------------ TMA staging
@@ -302,13 +326,14 @@ __device__ __forceinline__ bool tma_eligible(const Tile &t, int stage_bytes) {
 
 // Warp 0: start the bulk copies of tile `ti` into `stage` (nothing when the
 // tile is past the end or not eligible).
-__device__ __forceinline__ void issue_stage(const Tile *__restrict__ tiles, long long ti,
-                                            long long n, unsigned char *stage, uint32_t bar,
+__device__ __forceinline__ void issue_stage(const PlanList &list, long long ti, long long n,
+                                            unsigned char *stage, uint32_t bar,
                                             int stage_bytes) {
     if (ti >= n)
         return;
     const int lane = threadIdx.x & 31;
-    const Tile t = tiles[ti];
+    const PairInfo *unused;
+    const Tile t = *locate_copy(list, ti, unused);
     if (!tma_eligible(t, stage_bytes))
         return;
     const int L = t.rows * kind_esz(t.kind);
@@ -712,23 +737,36 @@ template <int U, int THREADS> struct MinBlocks {
 
 template <int THREADS, int U, int PATHS>
 __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
-    scatter_kernel(const Tile *__restrict__ tiles, const long long *__restrict__ n_tiles_p,
-                   long long capacity, const PairInfo *__restrict__ pairs, int td) {
+    scatter_kernel(const __grid_constant__ PlanList list, int td) {
     extern __shared__ __align__(128) unsigned char smem[];
-    long long n = *n_tiles_p;
-    if (n > capacity)
-        n = capacity;
-    for (long long ti = blockIdx.x; ti < n; ti += gridDim.x) {
-        if (threadIdx.x == 0 && ti + gridDim.x < n)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(tiles + ti + gridDim.x));
-        const Tile t = tiles[ti];
-        const uint32_t k = t.kind;
-        if ((PATHS & PATH_COPY) && !(k & (KIND_TRANS | KIND_SCALED)))
-            copy_tile<THREADS, U>(t);
-        else if ((PATHS & PATH_TRANSPOSE) && (k & KIND_TRANS) && !(k & KIND_SCALED))
-            transpose_dispatch<THREADS>(t, smem, td);
-        else if (PATHS & PATH_SCALED)
-            scaled_dispatch<THREADS>(t, pairs, smem, td);
+    constexpr int NWARP = THREADS / 32;
+    const int warp = threadIdx.x >> 5;
+    // phase 1: plain copies, one warp per tile, so a CTA keeps NWARP tiles in
+    // flight however small the pieces are
+    if (PATHS & PATH_COPY) {
+        const long long GW = (long long)gridDim.x * NWARP;
+        for (long long ti = (long long)blockIdx.x * NWARP + warp; ti < list.total_copy;
+             ti += GW) {
+            const PairInfo *pairs;
+            if ((threadIdx.x & 31) == 0 && ti + GW < list.total_copy) {
+                const PairInfo *unused;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, ti + GW, unused)));
+            }
+            const Tile t = *locate_copy(list, ti, pairs);
+            copy_tile<1, U>(t, 0);
+        }
+    }
+    // phase 2: transposed and scaled tiles, one CTA per tile
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
+        for (long long ti = blockIdx.x; ti < list.total_cta; ti += gridDim.x) {
+            const PairInfo *pairs;
+            const Tile t = *locate_cta(list, ti, pairs);
+            const uint32_t k = t.kind;
+            if ((PATHS & PATH_TRANSPOSE) && (k & KIND_TRANS) && !(k & KIND_SCALED))
+                transpose_dispatch<THREADS>(t, smem, td);
+            else if (PATHS & PATH_SCALED)
+                scaled_dispatch<THREADS>(t, pairs, smem, td);
+        }
     }
 }
 
@@ -741,16 +779,13 @@ constexpr uint64_t STAGE_WAIT_LIMIT_NS = 2000000000ull; // 2 s
 
 template <int THREADS, int U, int PATHS, int S>
 __global__ void __launch_bounds__(THREADS, 1)
-    scatter_staged_kernel(const Tile *__restrict__ tiles, const long long *__restrict__ n_tiles_p,
-                          long long capacity, const PairInfo *__restrict__ pairs, int td,
-                          int stage_bytes, int *__restrict__ status) {
+    scatter_staged_kernel(const __grid_constant__ PlanList list, int td, int stage_bytes) {
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     unsigned char *stages = smem + 128;
     unsigned char *direct = stages + (size_t)S * (size_t)stage_bytes;
-    long long n = *n_tiles_p;
-    if (n > capacity)
-        n = capacity;
+    const long long n = list.total_copy;
+    int *status = list.status;
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         for (int k = 0; k < S; ++k)
@@ -761,12 +796,13 @@ __global__ void __launch_bounds__(THREADS, 1)
     const long long G = gridDim.x;
     if (warp == 0)
         for (int k = 0; k < S; ++k)
-            issue_stage(tiles, blockIdx.x + k * G, n, stages + (size_t)k * stage_bytes,
+            issue_stage(list, blockIdx.x + k * G, n, stages + (size_t)k * stage_bytes,
                         smem_addr(&bars[k]), stage_bytes);
     uint32_t phase = 0;
     int st = 0;
     for (long long ti = blockIdx.x; ti < n; ti += G) {
-        const Tile t = tiles[ti];
+        const PairInfo *pairs;
+        const Tile t = *locate_copy(list, ti, pairs);
         unsigned char *stage = stages + (size_t)st * stage_bytes;
         const uint32_t bar = smem_addr(&bars[st]);
         if ((PATHS & PATH_COPY) && tma_eligible(t, stage_bytes)) {
@@ -783,24 +819,29 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             phase ^= 1u << st;
             consume_stage<THREADS, U>(t, stage);
-        } else if ((PATHS & PATH_COPY) && !(t.kind & (KIND_TRANS | KIND_SCALED))) {
-            copy_tile<THREADS, U>(t);
-        } else if ((PATHS & PATH_TRANSPOSE) && (t.kind & KIND_TRANS) &&
-                   !(t.kind & KIND_SCALED)) {
-            transpose_dispatch<THREADS>(t, direct, td);
-        } else if (PATHS & PATH_SCALED) {
-            scaled_dispatch<THREADS>(t, pairs, direct, td);
+        } else {
+            copy_tile<THREADS / 32, U>(t, warp);
         }
         __syncthreads(); // the stage is free again
         if (warp == 0)
-            issue_stage(tiles, ti + (long long)S * G, n, stage, bar, stage_bytes);
+            issue_stage(list, ti + (long long)S * G, n, stage, bar, stage_bytes);
         st = (st + 1 == S) ? 0 : st + 1;
+    }
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
+        for (long long ti = blockIdx.x; ti < list.total_cta; ti += G) {
+            const PairInfo *pairs;
+            const Tile t = *locate_cta(list, ti, pairs);
+            if ((PATHS & PATH_TRANSPOSE) && (t.kind & KIND_TRANS) && !(t.kind & KIND_SCALED))
+                transpose_dispatch<THREADS>(t, direct, td);
+            else if (PATHS & PATH_SCALED)
+                scaled_dispatch<THREADS>(t, pairs, direct, td);
+        }
     }
 }
 
 template <typename K>
-cudaError_t launch_kernel(K k, const PlanDevice &d, const ScatterConfig &cfg, size_t smem,
-                          cudaStream_t s, bool staged) {
+cudaError_t prepare(K k, const ScatterConfig &cfg, size_t smem, long long total,
+                    unsigned &grid_out) {
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -818,51 +859,60 @@ cudaError_t launch_kernel(K k, const PlanDevice &d, const ScatterConfig &cfg, si
     const long long resident = (long long)cfg.sm_count * occ;
     if (cfg.sm_count > 0 && grid > resident)
         grid = resident;
-    if (grid < 1)
-        grid = 1;
-    if (staged)
-        ((void (*)(const Tile *, const long long *, long long, const PairInfo *, int, int,
-                   int *))k)<<<(unsigned)grid, cfg.threads, smem, s>>>(
-            d.tiles, d.n_tiles, d.tile_capacity, d.pairs, cfg.tile_dim, cfg.stage_bytes,
-            d.status);
-    else
-        ((void (*)(const Tile *, const long long *, long long, const PairInfo *,
-                   int))k)<<<(unsigned)grid, cfg.threads, smem, s>>>(
-            d.tiles, d.n_tiles, d.tile_capacity, d.pairs, cfg.tile_dim);
+    if (grid > total)
+        grid = total;
+    grid_out = (unsigned)(grid < 1 ? 1 : grid);
+    return cudaSuccess;
+}
+
+template <int THREADS, int U, int PATHS, int S>
+cudaError_t launch_staged(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
+    auto k = scatter_staged_kernel<THREADS, U, PATHS, S>;
+    const size_t smem = staged_smem_bytes(cfg);
+    unsigned grid = 0;
+    cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim, cfg.stage_bytes);
     return cudaGetLastError();
 }
 
 template <int THREADS, int U, int PATHS>
-cudaError_t launch_t(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+cudaError_t launch_t(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
     if ((PATHS & PATH_COPY) && cfg.stages >= 2) {
-        const size_t smem = staged_smem_bytes(cfg);
         switch (cfg.stages) {
-        case 2: return launch_kernel(scatter_staged_kernel<THREADS, U, PATHS, 2>, d, cfg, smem, s, true);
-        case 3: return launch_kernel(scatter_staged_kernel<THREADS, U, PATHS, 3>, d, cfg, smem, s, true);
-        default: return launch_kernel(scatter_staged_kernel<THREADS, U, PATHS, 4>, d, cfg, smem, s, true);
+        case 2: return launch_staged<THREADS, U, PATHS, 2>(list, cfg, s);
+        case 3: return launch_staged<THREADS, U, PATHS, 3>(list, cfg, s);
+        default: return launch_staged<THREADS, U, PATHS, 4>(list, cfg, s);
         }
     }
-    return launch_kernel(scatter_kernel<THREADS, U, PATHS>, d, cfg, cfg.smem_bytes, s, false);
+    auto k = scatter_kernel<THREADS, U, PATHS>;
+    unsigned grid = 0;
+    cudaError_t e = prepare(k, cfg, cfg.smem_bytes, list.total_copy + list.total_cta, grid);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, THREADS, cfg.smem_bytes, s>>>(list, cfg.tile_dim);
+    return cudaGetLastError();
 }
 
 template <int THREADS, int PATHS>
-cudaError_t launch_u(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+cudaError_t launch_u(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
     switch (cfg.unroll) {
-    case 1: return launch_t<THREADS, 1, PATHS>(d, cfg, s);
-    case 2: return launch_t<THREADS, 2, PATHS>(d, cfg, s);
-    default: return launch_t<THREADS, 4, PATHS>(d, cfg, s);
+    case 1: return launch_t<THREADS, 1, PATHS>(l, cfg, s);
+    case 2: return launch_t<THREADS, 2, PATHS>(l, cfg, s);
+    default: return launch_t<THREADS, 4, PATHS>(l, cfg, s);
     }
 }
 
 template <int THREADS>
-cudaError_t launch_p(const PlanDevice &d, const ScatterConfig &cfg, cudaStream_t s) {
+cudaError_t launch_p(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
     if (cfg.paths & PATH_SCALED)
-        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(d, cfg, s);
+        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(l, cfg, s);
     if (cfg.paths == PATH_COPY)
-        return launch_u<THREADS, PATH_COPY>(d, cfg, s);
+        return launch_u<THREADS, PATH_COPY>(l, cfg, s);
     if (cfg.paths == PATH_TRANSPOSE)
-        return launch_u<THREADS, PATH_TRANSPOSE>(d, cfg, s);
-    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(d, cfg, s);
+        return launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
+    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
 }
 
 } // namespace
@@ -880,13 +930,15 @@ size_t staged_smem_bytes(const ScatterConfig &cfg) {
     return 128 + (size_t)cfg.stages * (size_t)cfg.stage_bytes + cfg.trans_bytes;
 }
 
-cudaError_t launch_scatter(const PlanDevice &d, const ScatterConfig &cfg,
+cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,
                            cudaStream_t stream) {
-    if (cfg.grid <= 0)
+    if (cfg.grid <= 0 || list.n < 1 || list.n > kMaxPlansPerLaunch)
         return cudaErrorInvalidConfiguration;
+    if (list.total_copy + list.total_cta <= 0)
+        return cudaSuccess;
     switch (cfg.threads) {
-    case 512: return launch_p<512>(d, cfg, stream);
-    default: return launch_p<256>(d, cfg, stream);
+    case 512: return launch_p<512>(list, cfg, stream);
+    default: return launch_p<256>(list, cfg, stream);
     }
 }
 

@@ -180,6 +180,13 @@ g2g_status g2g_plan_create_batch(int32_t n_pairs,
  * g2g_plan_capture_graph was called. */
 g2g_status g2g_plan_execute(g2g_plan *plan, void *stream);
 
+/* Executes several plans as ONE launch of the persistent gather-scatter
+ * (the concatenation of their work lists; up to 256 plans per launch, more
+ * are split into further launches). Plans must live on one device and their
+ * destinations must not overlap. Used for continuous batching of cached
+ * plans. */
+g2g_status g2g_plans_execute(int32_t n_plans, g2g_plan *const *plans, void *stream);
+
 /* Captures one execution into a CUDA graph; later executes replay it. */
 g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream);
 
@@ -221,6 +228,71 @@ g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a,
                           const int32_t *splits_b, int32_t n_b,
                           int32_t *start_index, int32_t *end_index,
                           void *stream);
+
+/* ---- serving: continuous batching ------------------------------------- */
+
+/* A request loop for transforms of device-resident layouts (no counterpart
+ * in the reference, which serves one collective call at a time). Requests
+ * are queued by g2g_server_submit and admitted while the bytes of admitted,
+ * unfinished requests (source + destination) stay within the HBM budget;
+ * a dispatcher thread launches all admissible queued requests as ONE launch
+ * (g2g_plans_execute over their cached plans) on one of several streams, so
+ * requests that arrive while others are on the GPU start as soon as a
+ * launch slot and budget free up and overlap with them on the device. */
+typedef struct g2g_server g2g_server;
+
+typedef struct g2g_server_config {
+    int64_t hbm_budget_bytes;      /* admission budget (0 = 120 GB)              */
+    int32_t max_launches_in_flight;/* concurrent launches / streams (0 = 3)      */
+    int32_t max_batch_requests;    /* requests per launch, 1..256 (0 = 256);
+                                      1 gives plain per-request launches        */
+    int32_t plan_cache_entries;    /* cached plans (0 = 4096)                    */
+    int32_t reserved[3];
+} g2g_server_config;
+
+typedef struct g2g_request_times {
+    int64_t submit_ns;    /* steady clock, when the request was queued   */
+    int64_t launch_ns;    /* when its launch was issued                  */
+    int64_t complete_ns;  /* when its launch was seen complete           */
+    int64_t bytes;        /* m*n*sizeof(T) of the request                */
+    int32_t status;       /* g2g_status of the request                   */
+    int32_t batch_size;   /* requests in the launch that carried it      */
+} g2g_request_times;
+
+typedef struct g2g_server_stats {
+    int64_t submitted, completed, launches, plan_cache_hits, plan_cache_misses;
+    int64_t bytes_completed;
+    int64_t inflight_bytes_peak;
+} g2g_server_stats;
+
+g2g_status g2g_server_create(const g2g_server_config *config, g2g_server **server);
+
+/* Queues a transform; *ticket identifies it. Fails with G2G_ERROR_BUDGET if
+ * the request alone exceeds the budget. Planning happens here (cached). */
+g2g_status g2g_server_submit(g2g_server *server, const g2g_layout_desc *initial,
+                             const g2g_layout_desc *final_, g2g_dtype dtype,
+                             const g2g_op *op, uint64_t *ticket);
+
+/* Waits up to timeout_us (< 0: forever) for a request; G2G_ERROR_NOT_READY if
+ * it is still pending. `times` may be NULL. A finished ticket is released
+ * by this call. */
+g2g_status g2g_server_wait(g2g_server *server, uint64_t ticket, int64_t timeout_us,
+                           g2g_request_times *times);
+
+/* Open-loop replay: submits request k (pair pair_index[k] of the given
+ * layout pairs) at arrival_s[k] seconds after the call starts, from a native
+ * thread, then waits for all and fills times[k]. */
+g2g_status g2g_server_replay(g2g_server *server, int32_t n_pairs,
+                             const g2g_layout_desc *initials,
+                             const g2g_layout_desc *finals, const g2g_dtype *dtypes,
+                             const g2g_op *ops, int64_t n_requests,
+                             const int32_t *pair_index, const double *arrival_s,
+                             g2g_request_times *times);
+
+g2g_status g2g_server_get_stats(const g2g_server *server, g2g_server_stats *stats);
+
+/* Finishes every queued request, then frees the server and its plans. */
+g2g_status g2g_server_destroy(g2g_server *server);
 
 #ifdef __cplusplus
 } /* extern "C" */
