@@ -161,6 +161,8 @@ SIGNATURES = [
     ("g2g_plan_destroy", C.c_int, [_VP]),
     ("g2g_transform", C.c_int,
      [C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op), _VP]),
+    ("g2g_transform_noalloc", C.c_int,
+     [C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op), _VP]),
     ("g2g_transform_batch", C.c_int,
      [C.c_int32, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.POINTER(C.c_int),
       C.POINTER(Op), _VP]),

@@ -1070,3 +1070,38 @@ g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a, const int32_t *s
 }
 
 } // extern "C"
+
+namespace g2g {
+
+g2g_status build_host_image(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                            g2g_dtype dtype, const g2g_op *op, HostPlanImage *out) {
+    if (!out)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "plan image output is NULL");
+    g2g_plan pl;
+    pl.n_pairs = 1;
+    pl.tuning = default_tuning();
+    pl.host.resize(1);
+    G2G_TRY(build_pair(initial, final_, (int)dtype, op, 0, pl.host[0]));
+    assemble(pl);
+    G2G_TRY(bind_device(pl));
+    G2G_CUDA(cudaGetDevice(&pl.device));
+    G2G_CUDA(cudaDeviceGetAttribute(&pl.sm_count, cudaDevAttrMultiProcessorCount, pl.device));
+    int64_t capacity = 0;
+    for (const PairHost &p : pl.host)
+        capacity += tile_capacity_bound(p, pl.tuning);
+    out->device = pl.device;
+    out->pairs = pl.pinfo;
+    out->splits = pl.splits;
+    out->src_tables = pl.src_tables;
+    out->dst_tables = pl.dst_tables;
+    out->n_parts = pl.n_parts;
+    out->n_cells = pl.n_cells;
+    out->max_cells_per_pair = pl.max_cells_per_pair;
+    out->tile_capacity = std::max<int64_t>(capacity, 1);
+    out->bytes_moved = pl.bytes_moved;
+    pl.n_tiles = out->tile_capacity; // grid bound only; the launch uses exact counts
+    out->cfg = scatter_config(pl);
+    return G2G_SUCCESS;
+}
+
+} // namespace g2g

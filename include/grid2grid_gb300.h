@@ -217,6 +217,24 @@ g2g_status g2g_transform_batch(int32_t n_pairs,
                                const g2g_dtype *dtypes, const g2g_op *ops,
                                void *stream);
 
+/* The one-shot transform of g2g_transform for callers that cannot allocate
+ * device memory (an application that gives all of HBM to its own pool and
+ * forbids other allocations, a process under a strict memory quota, a
+ * latency-critical loop that cannot take cudaFree's implicit device
+ * synchronisation). No counterpart in the reference. It calls no CUDA or
+ * library allocation routine: plan metadata and the work list live in a
+ * fixed 32 MiB device array inside the library, held on every GPU where the
+ * library's device code is loaded until the process exits. Limits: a
+ * transform needing more metadata than the array holds is rejected with
+ * G2G_ERROR_OUT_OF_MEMORY before any device work; all calls share the array,
+ * so calls that overlap on the GPU race (the call returns after its
+ * transform has completed; issue calls one at a time per device). The first
+ * call on a device resolves the array's address; make it before any stream
+ * capture. One dtype and op as in g2g_transform; `op` may be NULL. */
+g2g_status g2g_transform_noalloc(const g2g_layout_desc *initial,
+                                 const g2g_layout_desc *final_, g2g_dtype dtype,
+                                 const g2g_op *op, void *stream);
+
 /* ---- grid cover -------------------------------------------------------- */
 
 /* grid_cover of two split vectors (get_decomp_cover, grid_cover.cpp:54-121),
