@@ -315,8 +315,8 @@ g2g_status check_tuning(const g2g_tuning &t) {
     if (t.tile_bytes < 512 || t.tile_bytes > (1 << 24))
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_bytes %d outside [512, 16M]",
                     t.tile_bytes);
-    if (t.tile_dim != 16 && t.tile_dim != 32 && t.tile_dim != 64)
-        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_dim must be 16, 32 or 64");
+    if (t.tile_dim != 16 && t.tile_dim != 32)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_dim must be 16 or 32");
     if (t.threads != 256 && t.threads != 512)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: threads must be 256 or 512");
     if (t.unroll != 1 && t.unroll != 2 && t.unroll != 4)
@@ -499,6 +499,12 @@ void assemble(g2g_plan &pl) {
         pi.tile_rows = (int32_t)std::max(1, 4096 / p.esz);
         pi.tile_bytes = pl.tuning.tile_bytes;
         pi.tile_dim = pl.tuning.tile_dim;
+        {
+            bool all_trans = !p.a.blocks.empty();
+            for (const HBlock &b : p.a.blocks)
+                all_trans = all_trans && b.trans;
+            pi.row_major_cells = all_trans ? 1 : 0;
+        }
         pi.alpha[0] = p.alpha[0];
         pi.alpha[1] = p.alpha[1];
         pi.beta[0] = p.beta[0];
@@ -894,7 +900,7 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
     const g2g_tuning start = plan->tuning;
     std::vector<g2g_tuning> cands;
     const int tile_bytes_opts[] = {16 * 1024, 32 * 1024, 64 * 1024};
-    const int tile_dim_opts[] = {32, 64};
+    const int tile_dim_opts[] = {16, 32};
     const int threads_opts[] = {256, 512};
     const int unroll_opts[] = {2, 4};
     const int ctas_opts[] = {2, 4, 8};

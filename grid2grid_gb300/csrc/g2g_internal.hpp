@@ -59,6 +59,9 @@ struct PairInfo {
     int32_t tile_rows;         // non-transposed tile: max rows per tile
     int32_t tile_bytes;        // non-transposed tile: target bytes per tile
     int32_t tile_dim;          // transposed tile edge (elements)
+    int32_t row_major_cells;   // 1: cells numbered row part by row part (pairs
+                               // whose source is read transposed), 0: column
+                               // strips (row parts fastest)
     double alpha[2];
     double beta[2];
 };

@@ -62,7 +62,7 @@ struct ScatterConfig {
     int grid = 0;            // CTAs (persistent); 0 = SM count x ctas_per_sm
     int ctas_per_sm = 4;
     int sm_count = 0;        // for the residency clamp of the persistent grid
-    int tile_dim = 32;       // transposed tile edge (16, 32 or 64)
+    int tile_dim = 32;       // transposed tile edge (16 or 32)
     size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)

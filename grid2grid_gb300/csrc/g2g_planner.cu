@@ -96,6 +96,17 @@ __global__ void merge_parts_kernel(const PairInfo *__restrict__ pairs,
     }
 }
 
+__device__ inline void cell_coords(const PairInfo &p, long long cidx, int nrp, int ncp, int &u,
+                                   int &v) {
+    if (p.row_major_cells) {
+        u = (int)(cidx / ncp);
+        v = (int)(cidx - (long long)u * ncp);
+    } else {
+        v = (int)(cidx / nrp);
+        u = (int)(cidx - (long long)v * nrp);
+    }
+}
+
 __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
                                   int len_c, int &tr, int &tc) {
     if (kind & KIND_TRANS) {
@@ -131,9 +142,11 @@ __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pair
          cidx += (long long)gridDim.x * blockDim.x) {
         // column-strip order: the row parts of one column part are
         // consecutive, so pieces that share destination (and source) columns
-        // are in flight together and their boundary sectors meet in L2
-        int v = (int)(cidx / nrp);
-        int u = (int)(cidx - (long long)v * nrp);
+        // are in flight together and their boundary sectors meet in L2. A
+        // transposed source is stored the other way round, so its pairs walk
+        // row parts instead, keeping consecutive reads in one source column.
+        int u, v;
+        cell_coords(p, cidx, nrp, ncp, u, v);
         Part pr = parts[p.row_parts + u];
         Part pc = parts[p.col_parts + v];
         long long cnt = 0;
@@ -262,8 +275,8 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
     const long long warps_total = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long cidx = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
          cidx < n_cells; cidx += warps_total) {
-        int v = (int)(cidx / nrp); // column-strip order, as in cell_tiles_kernel
-        int u = (int)(cidx - (long long)v * nrp);
+        int u, v; // cell order as in cell_tiles_kernel
+        cell_coords(p, cidx, nrp, ncp, u, v);
         Part pr = parts[p.row_parts + u];
         Part pc = parts[p.col_parts + v];
         if (pr.len <= 0 || pc.len <= 0)

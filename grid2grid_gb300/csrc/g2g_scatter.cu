@@ -15,10 +15,11 @@
 //                    by whole words. Loads and stores are 128-bit; only the
 //                    head and tail chunk of a column store single words.
 //                    (memory_utils.hpp:41-77)
-//  * transpose_tile  plain, transposed (+ conjugated): a tile staged through
+//  * transposed      plain, transposed (+ conjugated): a tile staged through
 //                    shared memory with a padded pitch, loaded coalesced along
 //                    the source's storage columns and stored coalesced along
-//                    the destination's columns (memory_utils.hpp:124-184).
+//                    the destination's columns, the next tile's loads issued
+//                    before the current one is stored (memory_utils.hpp:124-184).
 //  * scaled tiles    dst = beta*dst + alpha*op(src) in the element type with
 //                    the rounding of the reference's host arithmetic: every
 //                    product and sum rounded separately, complex products in
@@ -450,65 +451,6 @@ __device__ __forceinline__ void consume_stage(const Tile &t, const unsigned char
     }
 }
 
-// ------------------------------------------------------ plain transposed tile
-template <typename W, int NWE> struct ElemW {
-    W w[NWE];
-};
-
-template <int THREADS, typename W, int NWE>
-__device__ __forceinline__ void transpose_tile(const Tile &t, unsigned char *smem_raw,
-                                               int td, bool conj) {
-    constexpr int NWARP = THREADS / 32;
-    constexpr int E = (int)sizeof(W) * NWE;
-    typedef ElemW<W, NWE> El;
-    El *smem = reinterpret_cast<El *>(smem_raw);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int R = t.rows, C = t.cols;
-    const int pitch = td + 1;
-    // load: storage column r (final row r) holds C contiguous elements
-    for (int c0 = 0; c0 < C; c0 += 32) {
-        const int c = c0 + lane;
-        for (int rb = warp; rb < R; rb += 4 * NWARP) {
-            El v[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int r = rb + i * NWARP;
-                if (r < R && c < C) {
-                    const uint64_t p = t.src + (uint64_t)((long long)r * t.src_ld +
-                                                          (long long)c * E);
-#pragma unroll
-                    for (int k = 0; k < NWE; ++k)
-                        v[i].w[k] = ldg_w<W>(p + (uint64_t)k * sizeof(W));
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int r = rb + i * NWARP;
-                if (r < R && c < C)
-                    smem[r * pitch + c] = v[i];
-            }
-        }
-    }
-    __syncthreads();
-    // store: destination column c, lanes along its rows
-    for (int r0 = 0; r0 < R; r0 += 32) {
-        const int r = r0 + lane;
-        if (r < R) {
-            for (int c = warp; c < C; c += NWARP) {
-                El e = smem[r * pitch + c];
-                if (conj)
-                    flip_top_sign(e.w[NWE - 1]);
-                const uint64_t p = t.dst + (uint64_t)((long long)c * t.dst_ld +
-                                                      (long long)r * E);
-#pragma unroll
-                for (int k = 0; k < NWE; ++k)
-                    st_w<W>(p + (uint64_t)k * sizeof(W), e.w[k]);
-            }
-        }
-    }
-    __syncthreads();
-}
-
 // --------------------------------------------------------------- scaled tiles
 struct cplxf {
     float x, y;
@@ -686,30 +628,157 @@ __device__ __forceinline__ void scaled_tile(const Tile &t, const PairInfo *pairs
     __syncthreads();
 }
 
-// ------------------------------------------------------------------ kernel
-template <int THREADS>
-__device__ __forceinline__ void transpose_dispatch(const Tile &t, unsigned char *smem,
-                                                   int td) {
+// ------------------------------------------- pipelined transposed tiles
+// One code path for every element size: each thread holds up to NE elements
+// of a tile as raw 16-byte register slots; the element size and alignment
+// (uniform per tile) pick 4/8/16-byte or split accesses. The CTA-level loop
+// issues the NEXT tile's loads into the slots before it stores the current
+// tile from shared memory, so loads stay in flight across the barriers.
+enum : int { EM_4 = 0, EM_8 = 1, EM_8_SPLIT = 2, EM_16 = 3, EM_16_SPLIT8 = 4, EM_16_SPLIT4 = 5 };
+
+__device__ __forceinline__ int elem_mode(const Tile &t) {
     const int esz = kind_esz(t.kind);
-    const bool conj = (t.kind & KIND_CONJ) != 0;
     const uint64_t a = t.src | t.dst | (uint64_t)t.src_ld | (uint64_t)t.dst_ld;
-    if (esz == 4) {
-        transpose_tile<THREADS, uint32_t, 1>(t, smem, td, conj);
-    } else if (esz == 8) {
-        if ((a & 7u) == 0)
-            transpose_tile<THREADS, unsigned long long, 1>(t, smem, td, conj);
-        else
-            transpose_tile<THREADS, uint32_t, 2>(t, smem, td, conj);
-    } else {
-        if ((a & 15u) == 0)
-            transpose_tile<THREADS, uint4, 1>(t, smem, td, conj);
-        else if ((a & 7u) == 0)
-            transpose_tile<THREADS, unsigned long long, 2>(t, smem, td, conj);
-        else
-            transpose_tile<THREADS, uint32_t, 4>(t, smem, td, conj);
+    if (esz == 4)
+        return EM_4;
+    if (esz == 8)
+        return (a & 7u) == 0 ? EM_8 : EM_8_SPLIT;
+    return (a & 15u) == 0 ? EM_16 : ((a & 7u) == 0 ? EM_16_SPLIT8 : EM_16_SPLIT4);
+}
+
+__device__ __forceinline__ uint4 ld_elem_raw(uint64_t a, int mode) {
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    switch (mode) {
+    case EM_4: v.x = ldg_w<uint32_t>(a); break;
+    case EM_8: {
+        const unsigned long long w = ldg_w<unsigned long long>(a);
+        v.x = (uint32_t)w;
+        v.y = (uint32_t)(w >> 32);
+        break;
+    }
+    case EM_8_SPLIT:
+        v.x = ldg_w<uint32_t>(a);
+        v.y = ldg_w<uint32_t>(a + 4);
+        break;
+    case EM_16: v = ldg_v4(a); break;
+    case EM_16_SPLIT8: {
+        const unsigned long long w0 = ldg_w<unsigned long long>(a);
+        const unsigned long long w1 = ldg_w<unsigned long long>(a + 8);
+        v = make_uint4((uint32_t)w0, (uint32_t)(w0 >> 32), (uint32_t)w1, (uint32_t)(w1 >> 32));
+        break;
+    }
+    default:
+        v = make_uint4(ldg_w<uint32_t>(a), ldg_w<uint32_t>(a + 4), ldg_w<uint32_t>(a + 8),
+                       ldg_w<uint32_t>(a + 12));
+        break;
+    }
+    return v;
+}
+
+__device__ __forceinline__ void st_elem_raw(uint64_t a, uint4 v, int mode) {
+    switch (mode) {
+    case EM_4: st_u32(a, v.x); break;
+    case EM_8:
+        st_w<unsigned long long>(a, (unsigned long long)v.x | ((unsigned long long)v.y << 32));
+        break;
+    case EM_8_SPLIT:
+        st_u32(a, v.x);
+        st_u32(a + 4, v.y);
+        break;
+    case EM_16: st_v4(a, v); break;
+    case EM_16_SPLIT8:
+        st_w<unsigned long long>(a, (unsigned long long)v.x | ((unsigned long long)v.y << 32));
+        st_w<unsigned long long>(a + 8, (unsigned long long)v.z | ((unsigned long long)v.w << 32));
+        break;
+    default:
+        st_u32(a, v.x);
+        st_u32(a + 4, v.y);
+        st_u32(a + 8, v.z);
+        st_u32(a + 12, v.w);
+        break;
     }
 }
 
+__device__ __forceinline__ void sts_elem(unsigned char *p, uint4 v, int esz) {
+    if (esz == 4)
+        *reinterpret_cast<uint32_t *>(p) = v.x;
+    else if (esz == 8)
+        *reinterpret_cast<uint2 *>(p) = make_uint2(v.x, v.y);
+    else
+        *reinterpret_cast<uint4 *>(p) = v;
+}
+
+__device__ __forceinline__ uint4 lds_elem(const unsigned char *p, int esz) {
+    if (esz == 4)
+        return make_uint4(*reinterpret_cast<const uint32_t *>(p), 0u, 0u, 0u);
+    if (esz == 8) {
+        const uint2 w = *reinterpret_cast<const uint2 *>(p);
+        return make_uint4(w.x, w.y, 0u, 0u);
+    }
+    return *reinterpret_cast<const uint4 *>(p);
+}
+
+__device__ __forceinline__ bool is_plain_transpose(const Tile &t) {
+    return (t.kind & KIND_TRANS) && !(t.kind & KIND_SCALED);
+}
+
+// Element i of this thread in a td x td tile (td a power of two): load view
+// (storage column r = final row, contiguous along c = final column).
+template <int THREADS, int NE>
+__device__ __forceinline__ void load_tile_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    const int td = 1 << td_shift;
+    const int mode = elem_mode(t);
+    const int esz = kind_esz(t.kind);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        const int idx = threadIdx.x + i * THREADS;
+        const int r = idx >> td_shift, c = idx & (td - 1);
+        if (idx < (td << td_shift) && r < t.rows && c < t.cols)
+            v[i] = ld_elem_raw(t.src + (uint64_t)((long long)r * t.src_ld + (long long)c * esz),
+                               mode);
+    }
+}
+
+template <int THREADS, int NE>
+__device__ __forceinline__ void slots_to_smem(const Tile &t, int td_shift, const uint4 (&v)[NE],
+                                              unsigned char *smem) {
+    const int td = 1 << td_shift;
+    const int esz = kind_esz(t.kind);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        const int idx = threadIdx.x + i * THREADS;
+        const int r = idx >> td_shift, c = idx & (td - 1);
+        if (idx < (td << td_shift) && r < t.rows && c < t.cols)
+            sts_elem(smem + (size_t)(r * (td + 1) + c) * esz, v[i], esz);
+    }
+}
+
+// Store view: destination column c (storage row), contiguous along r.
+template <int THREADS, int NE>
+__device__ __forceinline__ void smem_to_global(const Tile &t, int td_shift,
+                                               const unsigned char *smem) {
+    const int td = 1 << td_shift;
+    const int mode = elem_mode(t);
+    const int esz = kind_esz(t.kind);
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        const int idx = threadIdx.x + i * THREADS;
+        const int c = idx >> td_shift, r = idx & (td - 1);
+        if (idx < (td << td_shift) && r < t.rows && c < t.cols) {
+            uint4 e = lds_elem(smem + (size_t)(r * (td + 1) + c) * esz, esz);
+            if (conj) { // sign of the imaginary part: top word of the element
+                if (esz == 8)
+                    e.y ^= 0x80000000u;
+                else if (esz == 16)
+                    e.w ^= 0x80000000u;
+            }
+            st_elem_raw(t.dst + (uint64_t)((long long)c * t.dst_ld + (long long)r * esz), e, mode);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ kernel
 template <int THREADS>
 __device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *pairs,
                                                 unsigned char *smem, int td) {
@@ -730,10 +799,59 @@ enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
 // 512 (up to 128 registers) for U >= 4, so every variant keeps
 // U x 16 B x threads >= 32 KB of reads in flight per SM without spilling.
 template <int U, int THREADS> struct MinBlocks {
-    static constexpr int value = ((U <= 2 ? 1024 : 512) / THREADS) > 0
-                                     ? ((U <= 2 ? 1024 : 512) / THREADS)
-                                     : 1;
+    static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
 };
+
+// CTA-level tiles (transposed, scaled) of a launch, static striding, with the
+// next transposed tile's loads issued before the current tile is stored.
+template <int THREADS, int PATHS>
+__device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
+    constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
+    const int td_shift = td >= 32 ? 5 : 4;
+    const long long n = list.total_cta;
+    const long long G = gridDim.x;
+    uint4 v[NE];
+    long long ti = blockIdx.x;
+    Tile cur;
+    const PairInfo *cur_pairs = nullptr;
+    if (ti < n) {
+        cur = *locate_cta(list, ti, cur_pairs);
+        if ((PATHS & PATH_TRANSPOSE) && is_plain_transpose(cur))
+            load_tile_slots<THREADS, NE>(cur, td_shift, v);
+    }
+    while (ti < n) {
+        const long long next = ti + G;
+        // the next descriptor is read now and the one after is pulled into
+        // L2, so neither miss sits between the barriers
+        Tile nxt;
+        const PairInfo *nxt_pairs = nullptr;
+        if (next < n) {
+            nxt = *locate_cta(list, next, nxt_pairs);
+            if (threadIdx.x == 0 && next + G < n) {
+                const PairInfo *unused;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_cta(list, next + G, unused)));
+            }
+        }
+        __syncthreads(); // the previous tile is out of shared memory
+        if ((PATHS & PATH_TRANSPOSE) && is_plain_transpose(cur)) {
+            slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
+            __syncthreads();
+            if (next < n && is_plain_transpose(nxt))
+                load_tile_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
+            smem_to_global<THREADS, NE>(cur, td_shift, smem);
+        } else {
+            if (PATHS & PATH_SCALED)
+                scaled_dispatch<THREADS>(cur, cur_pairs, smem, td);
+            if ((PATHS & PATH_TRANSPOSE) && next < n && is_plain_transpose(nxt))
+                load_tile_slots<THREADS, NE>(nxt, td_shift, v);
+        }
+        if (next < n) {
+            cur = nxt;
+            cur_pairs = nxt_pairs;
+        }
+        ti = next;
+    }
+}
 
 template <int THREADS, int U, int PATHS>
 __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
@@ -757,17 +875,8 @@ __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
         }
     }
     // phase 2: transposed and scaled tiles, one CTA per tile
-    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
-        for (long long ti = blockIdx.x; ti < list.total_cta; ti += gridDim.x) {
-            const PairInfo *pairs;
-            const Tile t = *locate_cta(list, ti, pairs);
-            const uint32_t k = t.kind;
-            if ((PATHS & PATH_TRANSPOSE) && (k & KIND_TRANS) && !(k & KIND_SCALED))
-                transpose_dispatch<THREADS>(t, smem, td);
-            else if (PATHS & PATH_SCALED)
-                scaled_dispatch<THREADS>(t, pairs, smem, td);
-        }
-    }
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
+        cta_phase<THREADS, PATHS>(list, smem, td);
 }
 
 // The staged variant: a ring of S shared-memory stages filled by TMA bulk
@@ -827,16 +936,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             issue_stage(list, ti + (long long)S * G, n, stage, bar, stage_bytes);
         st = (st + 1 == S) ? 0 : st + 1;
     }
-    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
-        for (long long ti = blockIdx.x; ti < list.total_cta; ti += G) {
-            const PairInfo *pairs;
-            const Tile t = *locate_cta(list, ti, pairs);
-            if ((PATHS & PATH_TRANSPOSE) && (t.kind & KIND_TRANS) && !(t.kind & KIND_SCALED))
-                transpose_dispatch<THREADS>(t, direct, td);
-            else if (PATHS & PATH_SCALED)
-                scaled_dispatch<THREADS>(t, pairs, direct, td);
-        }
-    }
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
+        cta_phase<THREADS, PATHS>(list, direct, td);
 }
 
 template <typename K>

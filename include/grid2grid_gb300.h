@@ -121,7 +121,7 @@ typedef struct g2g_op {
  * g2g_plan_autotune picks them by measurement. */
 typedef struct g2g_tuning {
     int32_t tile_bytes;       /* target bytes per non-transposed tile       */
-    int32_t tile_dim;         /* edge (elements) of a transposed tile: 16/32/64 */
+    int32_t tile_dim;         /* edge (elements) of a transposed tile: 16 or 32 */
     int32_t ctas_per_sm;      /* persistent grid = ctas_per_sm x SM count   */
     int32_t threads;          /* threads per CTA: 128, 256 or 512           */
     int32_t unroll;           /* 16-byte chunks in flight per thread: 1,2,4,8 */
