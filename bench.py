@@ -154,6 +154,12 @@ def _allreduce_max(x: float, ws: int) -> float:
     return float(t.item())
 
 
+def replica_value(bytes_per_step: int, ms_per_step_max: float, world_size: int) -> float:
+    """Whole-job GB/s of independent replicas: every rank moves bytes_per_step
+    per step; the job's step time is the slowest rank's."""
+    return bytes_per_step * world_size / (ms_per_step_max * 1e-3) / 1e9
+
+
 def _cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -340,7 +346,7 @@ def run_ours(args):
         sampler.stop()
         clocks = sampler.summary(t_wall0, t_wall1)
     bytes_step = info.bytes_moved
-    value = bytes_step * ws / (ms_per_step * 1e-3) / 1e9
+    value = replica_value(bytes_step, ms_per_step, ws)
     peak, peak_kind = _peaks()
     achieved = info.bytes_min_traffic / (kernel_ms * 1e-3) / 1e9
     traffic = _profile_traffic("g2g_scatter", w.name)
