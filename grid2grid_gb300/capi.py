@@ -166,6 +166,7 @@ SIGNATURES = [
     ("g2g_transform_batch", C.c_int,
      [C.c_int32, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.POINTER(C.c_int),
       C.POINTER(Op), _VP]),
+    ("g2g_plan_cache_clear", C.c_int, []),
     ("g2g_grid_cover", C.c_int,
      [_I32P, C.c_int32, _I32P, C.c_int32, _I32P, _I32P, _VP]),
     ("g2g_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(_VP)]),

@@ -18,9 +18,12 @@
 #include <cctype>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <list>
 #include <map>
 #include <mutex>
+#include <unordered_map>
 #include <string>
 #include <vector>
 
@@ -771,6 +774,132 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
 
 } // namespace
 
+namespace {
+
+// Plans of the one-shot calls, keyed by a 128-bit signature of the
+// descriptors, dtypes and ops: repeated transforms between the same buffers
+// (the usual pattern of iterative callers) skip validation, upload and the
+// planner. Plans hold only metadata; the caller's buffers are never retained.
+// G2G_PLAN_CACHE_ENTRIES sets the capacity (0 turns the cache off).
+struct OneShotCache {
+    struct Entry {
+        g2g_plan *plan = nullptr;
+        int refs = 0;
+        std::list<g2g::Sig>::iterator lru;
+    };
+    std::mutex mu;
+    std::unordered_map<g2g::Sig, Entry, g2g::SigHash> map;
+    std::list<g2g::Sig> lru; // most recent first
+    int capacity = -1;
+    int cap() {
+        if (capacity < 0) {
+            const char *e = std::getenv("G2G_PLAN_CACHE_ENTRIES");
+            capacity = e ? std::max(0, std::atoi(e)) : 64;
+        }
+        return capacity;
+    }
+};
+OneShotCache g_cache;
+
+g2g::Sig one_shot_sig(int n, const g2g_layout_desc *init, const g2g_layout_desc *fin,
+                      const g2g_dtype *dtypes, g2g_dtype dtype, const g2g_op *ops) {
+    g2g::Sig sig;
+    sig.add(n);
+    for (int k = 0; k < n; ++k) {
+        g2g::add_layout(sig, &init[k]);
+        g2g::add_layout(sig, &fin[k]);
+        const g2g_dtype dt = dtypes ? dtypes[k] : dtype;
+        sig.add(dt);
+        g2g_op o;
+        std::memset(&o, 0, sizeof(o));
+        o.trans = 'N';
+        o.alpha[0] = 1.0;
+        if (ops) {
+            o.trans = ops[k].trans;
+            std::memcpy(o.alpha, ops[k].alpha, sizeof(o.alpha));
+            std::memcpy(o.beta, ops[k].beta, sizeof(o.beta));
+        }
+        sig.add(o.trans);
+        sig.add(o.alpha);
+        sig.add(o.beta);
+    }
+    return sig;
+}
+
+// plan (cached) + execute + wait: the reference's blocking transform call
+g2g_status one_shot(int n, const g2g_layout_desc *init, const g2g_layout_desc *fin,
+                    const g2g_dtype *dtypes, g2g_dtype dtype, const g2g_op *ops,
+                    void *stream) {
+    const bool cached = g_cache.cap() > 0 && n >= 1 && init && fin;
+    g2g_plan *plan = nullptr;
+    g2g::Sig sig;
+    if (cached) {
+        sig = one_shot_sig(n, init, fin, dtypes, dtype, ops);
+        std::lock_guard<std::mutex> lk(g_cache.mu);
+        auto it = g_cache.map.find(sig);
+        if (it != g_cache.map.end()) {
+            it->second.refs++;
+            g_cache.lru.erase(it->second.lru);
+            g_cache.lru.push_front(sig);
+            it->second.lru = g_cache.lru.begin();
+            plan = it->second.plan;
+        }
+    }
+    if (!plan) {
+        g2g_status st = create_plan(n, init, fin, dtypes, dtype, ops, &plan);
+        if (st != G2G_SUCCESS)
+            return st;
+        if (cached) {
+            std::vector<g2g_plan *> victims;
+            {
+                std::lock_guard<std::mutex> lk(g_cache.mu);
+                auto it = g_cache.map.find(sig);
+                if (it != g_cache.map.end()) { // planned concurrently by another thread
+                    victims.push_back(plan);
+                    plan = it->second.plan;
+                    it->second.refs++;
+                } else {
+                    g_cache.lru.push_front(sig);
+                    OneShotCache::Entry e;
+                    e.plan = plan;
+                    e.refs = 1;
+                    e.lru = g_cache.lru.begin();
+                    g_cache.map.emplace(sig, e);
+                    auto li = g_cache.lru.end();
+                    while ((int)g_cache.map.size() > g_cache.cap() && li != g_cache.lru.begin()) {
+                        --li;
+                        auto ci = g_cache.map.find(*li);
+                        if (ci != g_cache.map.end() && ci->second.refs == 0) {
+                            victims.push_back(ci->second.plan);
+                            g_cache.map.erase(ci);
+                            li = g_cache.lru.erase(li);
+                        }
+                    }
+                }
+            }
+            for (g2g_plan *v : victims)
+                g2g_plan_destroy(v);
+        }
+    }
+    g2g_status st = g2g_plan_execute(plan, stream);
+    if (st == G2G_SUCCESS) {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess)
+            st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
+    }
+    if (cached) {
+        std::lock_guard<std::mutex> lk(g_cache.mu);
+        auto it = g_cache.map.find(sig);
+        if (it != g_cache.map.end() && it->second.plan == plan)
+            it->second.refs--;
+        return st;
+    }
+    g2g_status st2 = g2g_plan_destroy(plan);
+    return st != G2G_SUCCESS ? st : st2;
+}
+
+} // namespace
+
 extern "C" {
 
 const char *g2g_last_error_string(void) { return t_last_error.c_str(); }
@@ -1010,31 +1139,38 @@ g2g_status g2g_plan_destroy(g2g_plan *plan) {
 
 g2g_status g2g_transform(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
                          g2g_dtype dtype, const g2g_op *op, void *stream) {
-    g2g_plan *plan = nullptr;
-    G2G_TRY(g2g_plan_create(initial, final_, dtype, op, stream, &plan));
-    g2g_status st = g2g_plan_execute(plan, stream);
-    if (st == G2G_SUCCESS) {
-        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
-        if (e != cudaSuccess)
-            st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
-    }
-    g2g_status st2 = g2g_plan_destroy(plan);
-    return st != G2G_SUCCESS ? st : st2;
+    return one_shot(1, initial, final_, nullptr, dtype, op, stream);
 }
 
 g2g_status g2g_transform_batch(int32_t n_pairs, const g2g_layout_desc *initials,
                                const g2g_layout_desc *finals, const g2g_dtype *dtypes,
                                const g2g_op *ops, void *stream) {
-    g2g_plan *plan = nullptr;
-    G2G_TRY(g2g_plan_create_batch(n_pairs, initials, finals, dtypes, ops, stream, &plan));
-    g2g_status st = g2g_plan_execute(plan, stream);
-    if (st == G2G_SUCCESS) {
-        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
-        if (e != cudaSuccess)
-            st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
+    if (!dtypes)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "dtypes is NULL");
+    return one_shot(n_pairs, initials, finals, dtypes, G2G_FLOAT32, ops, stream);
+}
+
+g2g_status g2g_plan_cache_clear(void) {
+    std::vector<g2g_plan *> victims;
+    {
+        std::lock_guard<std::mutex> lk(g_cache.mu);
+        for (auto it = g_cache.map.begin(); it != g_cache.map.end();) {
+            if (it->second.refs == 0) {
+                victims.push_back(it->second.plan);
+                g_cache.lru.erase(it->second.lru);
+                it = g_cache.map.erase(it);
+            } else {
+                ++it;
+            }
+        }
     }
-    g2g_status st2 = g2g_plan_destroy(plan);
-    return st != G2G_SUCCESS ? st : st2;
+    g2g_status st = G2G_SUCCESS;
+    for (g2g_plan *p : victims) {
+        g2g_status s2 = g2g_plan_destroy(p);
+        if (s2 != G2G_SUCCESS)
+            st = s2;
+    }
+    return st;
 }
 
 g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a, const int32_t *splits_b,

@@ -6,6 +6,7 @@
 #include "g2g_launch.hpp"
 
 #include <cstdint>
+#include <cstddef>
 #include <vector>
 
 namespace g2g {
@@ -38,5 +39,40 @@ struct HostPlanImage {
 // fills `out`; makes the device holding the blocks current.
 g2g_status build_host_image(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
                             g2g_dtype dtype, const g2g_op *op, HostPlanImage *out);
+
+// 128-bit signature of a request (two independent 64-bit FNV-1a streams).
+struct Sig {
+    uint64_t a = 1469598103934665603ull, b = 0x9e3779b97f4a7c15ull;
+    void add(const void *p, size_t n) {
+        const unsigned char *c = (const unsigned char *)p;
+        for (size_t i = 0; i < n; ++i) {
+            a = (a ^ c[i]) * 1099511628211ull;
+            b = (b ^ c[i]) * 0x100000001b3ull + 0x2545f4914f6cdd1dull;
+        }
+    }
+    template <typename T> void add(const T &v) { add(&v, sizeof(T)); }
+    bool operator==(const Sig &o) const { return a == o.a && b == o.b; }
+};
+struct SigHash {
+    size_t operator()(const Sig &s) const { return (size_t)(s.a ^ (s.b * 31)); }
+};
+
+inline void add_layout(Sig &s, const g2g_layout_desc *d) {
+    s.add(d->n_block_rows);
+    s.add(d->n_block_cols);
+    s.add(d->n_ranks);
+    s.add(d->n_reordering);
+    s.add(d->n_blocks);
+    if (d->rows_split && d->n_block_rows >= 0)
+        s.add(d->rows_split, sizeof(int32_t) * ((size_t)d->n_block_rows + 1));
+    if (d->cols_split && d->n_block_cols >= 0)
+        s.add(d->cols_split, sizeof(int32_t) * ((size_t)d->n_block_cols + 1));
+    if (d->owners && d->n_block_rows > 0 && d->n_block_cols > 0)
+        s.add(d->owners, sizeof(int32_t) * (size_t)d->n_block_rows * d->n_block_cols);
+    if (d->reordering && d->n_reordering > 0)
+        s.add(d->reordering, sizeof(int32_t) * (size_t)d->n_reordering);
+    if (d->blocks && d->n_blocks > 0)
+        s.add(d->blocks, sizeof(g2g_block_desc) * (size_t)d->n_blocks);
+}
 
 } // namespace g2g

@@ -37,41 +37,6 @@ int64_t now_ns() {
         .count();
 }
 
-// 128-bit signature of a request (two independent 64-bit FNV-1a streams).
-struct Sig {
-    uint64_t a = 1469598103934665603ull, b = 0x9e3779b97f4a7c15ull;
-    void add(const void *p, size_t n) {
-        const unsigned char *c = (const unsigned char *)p;
-        for (size_t i = 0; i < n; ++i) {
-            a = (a ^ c[i]) * 1099511628211ull;
-            b = (b ^ c[i]) * 0x100000001b3ull + 0x2545f4914f6cdd1dull;
-        }
-    }
-    template <typename T> void add(const T &v) { add(&v, sizeof(T)); }
-    bool operator==(const Sig &o) const { return a == o.a && b == o.b; }
-};
-struct SigHash {
-    size_t operator()(const Sig &s) const { return (size_t)(s.a ^ (s.b * 31)); }
-};
-
-void add_layout(Sig &s, const g2g_layout_desc *d) {
-    s.add(d->n_block_rows);
-    s.add(d->n_block_cols);
-    s.add(d->n_ranks);
-    s.add(d->n_reordering);
-    s.add(d->n_blocks);
-    if (d->rows_split && d->n_block_rows >= 0)
-        s.add(d->rows_split, sizeof(int32_t) * ((size_t)d->n_block_rows + 1));
-    if (d->cols_split && d->n_block_cols >= 0)
-        s.add(d->cols_split, sizeof(int32_t) * ((size_t)d->n_block_cols + 1));
-    if (d->owners && d->n_block_rows > 0 && d->n_block_cols > 0)
-        s.add(d->owners, sizeof(int32_t) * (size_t)d->n_block_rows * d->n_block_cols);
-    if (d->reordering && d->n_reordering > 0)
-        s.add(d->reordering, sizeof(int32_t) * (size_t)d->n_reordering);
-    if (d->blocks && d->n_blocks > 0)
-        s.add(d->blocks, sizeof(g2g_block_desc) * (size_t)d->n_blocks);
-}
-
 struct Req {
     g2g_plan *plan = nullptr;
     int *refs = nullptr; // the plan's cache reference count
@@ -85,7 +50,7 @@ struct CacheEntry {
     g2g_plan *plan = nullptr;
     int64_t bytes = 0;
     int refs = 0; // queued or in-flight requests using the plan
-    std::list<Sig>::iterator lru;
+    std::list<g2g::Sig>::iterator lru;
 };
 
 struct Launch;
@@ -104,8 +69,8 @@ struct g2g_server {
     int inflight_launches = 0;
     std::vector<cudaStream_t> streams;
     int next_stream = 0;
-    std::unordered_map<Sig, CacheEntry, SigHash> cache;
-    std::list<Sig> lru; // most recent at front
+    std::unordered_map<g2g::Sig, CacheEntry, g2g::SigHash> cache;
+    std::list<g2g::Sig> lru; // most recent at front
     std::thread dispatcher;
     bool stop = false;
     g2g_server_stats stats{};
@@ -209,9 +174,9 @@ void dispatch_loop(g2g_server *s) {
 g2g_status plan_for(g2g_server *s, const g2g_layout_desc *init, const g2g_layout_desc *fin,
                     g2g_dtype dtype, const g2g_op *op, g2g_plan **plan, int64_t *bytes,
                     int **refs) {
-    Sig sig;
-    add_layout(sig, init);
-    add_layout(sig, fin);
+    g2g::Sig sig;
+    g2g::add_layout(sig, init);
+    g2g::add_layout(sig, fin);
     sig.add(dtype);
     g2g_op o;
     std::memset(&o, 0, sizeof(o));

@@ -205,8 +205,12 @@ g2g_status g2g_plan_destroy(g2g_plan *plan);
 
 /* ---- one-shot transform ------------------------------------------------ */
 
-/* plan + execute + destroy: the reference's transform() call
- * (transform.cpp:126-164), which also re-plans on every call. */
+/* plan + execute, returning after the transform completed: the reference's
+ * blocking transform() call (transform.cpp:126-164). The reference re-plans
+ * on every call; here plans are cached, keyed by a 128-bit signature of the
+ * descriptors, dtype and op (at most G2G_PLAN_CACHE_ENTRIES plans, default
+ * 64, 0 = plan and free on every call). A cached plan holds device metadata
+ * only, never the caller's buffers. */
 g2g_status g2g_transform(const g2g_layout_desc *initial,
                          const g2g_layout_desc *final_, g2g_dtype dtype,
                          const g2g_op *op, void *stream);
@@ -234,6 +238,10 @@ g2g_status g2g_transform_batch(int32_t n_pairs,
 g2g_status g2g_transform_noalloc(const g2g_layout_desc *initial,
                                  const g2g_layout_desc *final_, g2g_dtype dtype,
                                  const g2g_op *op, void *stream);
+
+/* Frees every cached plan of g2g_transform / g2g_transform_batch that no
+ * call is using. */
+g2g_status g2g_plan_cache_clear(void);
 
 /* ---- grid cover -------------------------------------------------------- */
 

@@ -306,3 +306,26 @@ def test_full_size_round_trip_and_conservation():
     f = Lf.gather(dev_f.cpu().numpy())
     assert int(a.astype(np.uint64).sum()) == int(f.astype(np.uint64).sum())
     assert np.array_equal(np.sort(a, axis=None), np.sort(f, axis=None))
+
+
+def test_one_shot_plan_cache_reuse():
+    """Repeated one-shot transforms between the same buffers reuse the cached
+    plan; new source data must still come through, bit-exact."""
+    import torch
+    lib = capi.load()
+    rng = np.random.default_rng(321)
+    Li, Lf, ai, af = _random_case(rng, capi.COMPLEX64, "T", 333, 222, 5, ext_hi=100)
+    di = torch.from_numpy(ai).cuda()
+    df = torch.from_numpy(af).cuda()
+    dI, k1 = Li.desc(di.data_ptr())
+    dF, k2 = Lf.desc(df.data_ptr())
+    op = capi.make_op("T", 1.0, 0.0)
+    for trial in range(3):
+        src = Ls.fill_random(np.zeros(Li.arena_bytes, np.uint8), rng)
+        di.copy_(torch.from_numpy(src))
+        df.copy_(torch.from_numpy(af))
+        capi.check(lib.g2g_transform(C.byref(dI), C.byref(dF), capi.COMPLEX64, C.byref(op),
+                                     None))
+        want = T.port_run([Li], [Lf], [src], [af], [("T", 1.0, 0.0)])[0]
+        T.assert_arenas_equal(df.cpu().numpy(), want, Lf, what=f"cached one-shot {trial}")
+    capi.check(lib.g2g_plan_cache_clear())
