@@ -78,7 +78,8 @@ class Tuning(C.Structure):
         ("threads", C.c_int32),
         ("unroll", C.c_int32),
         ("stages", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("ring", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -298,6 +298,7 @@ g2g_tuning default_tuning() {
     t.threads = 256;
     t.unroll = 4;
     t.stages = -1; // TMA staging is opt-in (no faster on measured workloads)
+    t.ring = 1;
     return t;
 }
 
@@ -311,6 +312,7 @@ g2g_tuning merge_tuning(const g2g_tuning &base, const g2g_tuning *over) {
     if (over->threads) t.threads = over->threads;
     if (over->unroll) t.unroll = over->unroll;
     if (over->stages) t.stages = over->stages;
+    if (over->ring) t.ring = over->ring;
     return t;
 }
 
@@ -326,6 +328,8 @@ g2g_status check_tuning(const g2g_tuning &t) {
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: unroll must be 1, 2 or 4");
     if (t.stages != -1 && (t.stages < 2 || t.stages > 4))
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: stages must be -1 or 2..4");
+    if (t.ring != -1 && t.ring != 1)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ring must be -1 or 1");
     if (t.ctas_per_sm < 1 || t.ctas_per_sm > 32)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ctas_per_sm outside [1, 32]");
     return G2G_SUCCESS;
@@ -677,6 +681,7 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
                                     : 0;
     c.trans_bytes = c.smem_bytes;
     c.paths = pl.paths ? pl.paths : 1;
+    c.ring = pl.tuning.ring == 1 ? 1 : 0;
     c.stages = 0;
     if ((c.paths & 1) && pl.tuning.stages >= 2) {
         c.stage_bytes = g2g::stage_bytes_for(pl.tuning.tile_bytes);
@@ -685,6 +690,8 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
             --st;
         c.stages = st >= 2 ? st : 0;
     }
+    if (c.ring && g2g::ring_smem_bytes(c) > kMaxSmemPerCta)
+        c.ring = 0; // ring too large for one CTA: loads through registers
     return c;
 }
 
@@ -727,6 +734,8 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
     } else if (c.paths & 1) {
         c.stages = 0;
     }
+    if (c.ring && g2g::ring_smem_bytes(c) > kMaxSmemPerCta)
+        c.ring = 0;
     long long g = (long long)c.sm_count * plans[0]->tuning.ctas_per_sm;
     c.grid = (int)std::max<long long>(1, std::min(g, std::max<long long>(tiles, 1)));
     return c;
@@ -765,6 +774,15 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
     if (st != G2G_SUCCESS) {
         g2g_plan_destroy(pl);
         return st;
+    }
+    // Launch shape by the tiles the plan holds. Plain copies run best as 16
+    // warps per SM, each with its cp.async ring (3 stages of 2 KB in flight):
+    // more concurrent column streams lose DRAM locality. With CTA-level tiles
+    // as well, 256-thread CTAs keep more of those in flight.
+    if (pl->n_copy > 0) {
+        const bool cta_tiles = pl->n_tiles > pl->n_copy;
+        pl->tuning.threads = cta_tiles ? 256 : 512;
+        pl->tuning.ctas_per_sm = cta_tiles ? 3 : 2;
     }
     G2G_CUDA(cudaEventCreateWithFlags(&pl->done, cudaEventDisableTiming));
 
@@ -1028,12 +1046,13 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
     cudaStream_t s = (cudaStream_t)stream;
     const g2g_tuning start = plan->tuning;
     std::vector<g2g_tuning> cands;
-    const int tile_bytes_opts[] = {16 * 1024, 32 * 1024, 64 * 1024};
+    const int tile_bytes_opts[] = {4 * 1024, 8 * 1024, 16 * 1024, 32 * 1024, 64 * 1024};
     const int tile_dim_opts[] = {16, 32};
     const int threads_opts[] = {256, 512};
     const int unroll_opts[] = {2, 4};
     const int ctas_opts[] = {2, 4, 8};
     const int stage_opts[] = {-1, 2, 3, 4};
+    const int ring_opts[] = {1, -1};
     for (int tb : tile_bytes_opts)
         for (int td : tile_dim_opts) {
             if (!plan->any_trans && td != start.tile_dim)
@@ -1041,20 +1060,24 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
             for (int th : threads_opts)
                 for (int u : unroll_opts)
                     for (int c : ctas_opts)
-                        for (int sg : stage_opts) {
-                            if (th * c > 2048)
-                                continue;
-                            if (sg != -1 && !(plan->paths & 1))
-                                continue;
-                            g2g_tuning t = start;
-                            t.tile_bytes = tb;
-                            t.tile_dim = td;
-                            t.threads = th;
-                            t.unroll = u;
-                            t.ctas_per_sm = c;
-                            t.stages = sg;
-                            cands.push_back(t);
-                        }
+                        for (int sg : stage_opts)
+                            for (int rg : ring_opts) {
+                                if (th * c > 2048)
+                                    continue;
+                                if ((sg != -1 || rg != 1) && !(plan->paths & 1))
+                                    continue;
+                                if (sg != -1 && rg != 1)
+                                    continue;
+                                g2g_tuning t = start;
+                                t.tile_bytes = tb;
+                                t.tile_dim = td;
+                                t.threads = th;
+                                t.unroll = u;
+                                t.ctas_per_sm = c;
+                                t.stages = sg;
+                                t.ring = rg;
+                                cands.push_back(t);
+                            }
         }
     cudaEvent_t e0, e1;
     G2G_CUDA(cudaEventCreate(&e0));

@@ -66,6 +66,7 @@ struct ScatterConfig {
     size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
+    int ring = 0;            // plain copies through the per-warp cp.async ring
     int stage_bytes = 0;     // bytes per stage
     size_t trans_bytes = 0;  // shared memory for direct transposed / scaled tiles
 };
@@ -75,6 +76,8 @@ struct ScatterConfig {
 int stage_bytes_for(int tile_bytes);
 // Dynamic shared memory of the staged kernel.
 size_t staged_smem_bytes(const ScatterConfig &cfg);
+// Dynamic shared memory of the ring kernel.
+size_t ring_smem_bytes(const ScatterConfig &cfg);
 
 
 // Shared memory a transposed tile of edge `tile_dim` with elements of `esz`

@@ -7,14 +7,17 @@
 // strided block into the final owner's strided block.
 //
 // Three tile paths (uniform per tile, so no divergence):
-//  * copy_tile       plain, non-transposed: byte movement in 16-byte chunks
-//                    aligned to the DESTINATION. When source and destination
-//                    are misaligned differently (arbitrary strides), the
-//                    source window is assembled from this lane's 16-byte load
-//                    and the next lane's (warp shuffle), then funnel-shifted
-//                    by whole words. Loads and stores are 128-bit; only the
-//                    head and tail chunk of a column store single words.
-//                    (memory_utils.hpp:41-77)
+//  * plain copies    non-transposed: byte movement in 16-byte chunks aligned
+//                    to the DESTINATION, the chunks of a tile's columns walked
+//                    as one flat sequence by the lanes of a warp. When source
+//                    and destination are misaligned differently (arbitrary
+//                    strides), a chunk is assembled from two aligned source
+//                    blocks, funnel-shifted by whole words. Loads and stores
+//                    are 128-bit; only the head and tail chunk of a column
+//                    store single words (memory_utils.hpp:41-77). Two forms:
+//                    the source blocks staged by cp.async in a per-warp ring
+//                    in shared memory (ring kernel, default), or held in
+//                    registers (copy_tile).
 //  * transposed      plain, transposed (+ conjugated): a tile staged through
 //                    shared memory with a padded pitch, loaded coalesced along
 //                    the source's storage columns and stored coalesced along
@@ -104,21 +107,25 @@ __device__ __forceinline__ uint4 funnel_words(uint4 lo, uint4 hi, uint32_t q) {
 }
 
 // ------------------------------------------------------------ plain copy tile
-// Lanes of a warp form groups of `lpc` lanes (a power of two); a group walks
-// one column of the tile in 16-byte chunks aligned to the DESTINATION.
+// The tile's columns are cut into 16-byte chunks aligned to the DESTINATION;
+// the chunks of all columns form one flat sequence (column by column) that the
+// lanes walk 32 at a time, so a warp instruction covers 32 chunks whatever
+// the column length (no lane idles on short columns).
 //  * aligned tiles (source and destination at the same 16-byte phase in every
-//    column): lane kl copies chunks kl, kl + lpc, ... with one 128-bit load and
-//    one 128-bit store each;
-//  * otherwise every lane loads the aligned source block under its chunk and
-//    takes the next block from the next lane (warp shuffle) to funnel the
-//    window into place; the group's last lane only supplies that block, so a
-//    group stores lpc - 1 chunks per step and its last chunk is loaded again
-//    by the group's first lane on the next step.
+//    column): chunk k of a column is one 128-bit load and one 128-bit store;
+//  * otherwise destination chunk k is assembled from aligned source blocks k
+//    and k + 1 (funnel shift by whole words). Lane i loads block k; block
+//    k + 1 is the next chunk of the sequence, loaded by the next lane (warp
+//    shuffle) -- or, past lane 31, by lane 0 of the next unrolled step. Only
+//    the last lane of the last step loads its next block itself. A column is
+//    given as many chunks as aligned source blocks it touches, so its last
+//    chunk never needs the next column's block.
 // A column of a tile is at most 4 KB (tiles are cut at 4096 / sizeof(T)
 // rows), so per-chunk arithmetic is 32-bit, relative to the column's first
 // aligned destination chunk. Only 16-byte blocks overlapping the column are
 // read, so no access leaves the pages the column lives in; stores cover
 // exactly the column (word-masked head and tail chunks).
+// NWARP warps share a tile in runs of 32 * U consecutive chunks.
 template <int NWARP, int U>
 __device__ __forceinline__ void copy_tile(const Tile &t, const int warp) {
     const int lane = threadIdx.x & 31;
@@ -127,71 +134,93 @@ __device__ __forceinline__ void copy_tile(const Tile &t, const int warp) {
     if (L <= 0 || t.cols <= 0)
         return;
     const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
-    // destination chunks a column touches (exact if every column starts at
-    // the same 16-byte phase, else the bound over the four phases)
-    const int cpc = ((t.dst_ld & 15) == 0) ? (((int)(t.dst & 15u) + L + 15) >> 4)
-                                           : ((L + 27) >> 4);
-    // lanes per column: the smallest power of two whose step covers cpc
-    int lpc_shift = 0;
-    while (lpc_shift < 5 && ((1 << lpc_shift) - (aligned ? 0 : 1)) < cpc)
-        ++lpc_shift;
-    if (!aligned && lpc_shift == 0)
-        lpc_shift = 1;
-    const int lpc = 1 << lpc_shift;
-    const int step = aligned ? lpc : lpc - 1; // chunks stored per group step
-    const int cpw = 32 >> lpc_shift;          // columns per warp step
-    const int sub = lane >> lpc_shift;
-    const int kl = lane & (lpc - 1);
-    const bool stores = aligned || kl != lpc - 1;
-    const int col_step = NWARP * cpw;
-    const int warp_col0 = warp * cpw;
-    const int ncolit =
-        t.cols > warp_col0 ? (t.cols - warp_col0 + col_step - 1) / col_step : 0;
-    const int nkit = (cpc + step - 1) / step;
-    const int my_col0 = warp_col0 + sub;
-
-    int colit = 0, kit = 0;
-    while (colit < ncolit) { // warp-uniform
+    // chunks per column: the aligned source blocks a column touches from the
+    // block under its first destination chunk (exact when every column has
+    // the same 16-byte phases, else the bound over all phases: element
+    // addresses are 4-byte aligned, so the source lead is at most 24 bytes)
+    int cpc;
+    if (((t.dst_ld | t.src_ld) & 15) == 0) {
+        const int d0 = (int)(t.dst & 15u);
+        const int sh = (int)((t.src - (uint64_t)d0) & 15u);
+        cpc = (sh + d0 + L + 15) >> 4;
+    } else {
+        cpc = aligned ? ((L + 27) >> 4) : ((L + 39) >> 4);
+    }
+    const int total = t.cols * cpc;
+    // flat chunk index of this lane: run r = i * NWARP + warp, idx = r * 32U + u * 32 + lane
+    int col, k;
+    {
+        const int idx = warp * 32 * U + lane;
+        col = idx / cpc;
+        k = idx - col * cpc;
+    }
+    const int dq = 32 / cpc, dr = 32 - dq * cpc;                 // +32 chunks
+    const int skip = (NWARP - 1) * 32 * U;                       // to this warp's next run
+    const int sq = skip / cpc, sr = skip - sq * cpc;
+    for (int base = warp * 32 * U; base < total; base += NWARP * 32 * U) { // warp-uniform
         uint4 lo[U];
+        uint4 ex;
         uint64_t chunk[U];
         uint32_t qm[U]; // bits 0-3 store mask, bits 4-5 word shift
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int c = my_col0 + colit * col_step;
-            const bool colok = (colit < ncolit) && (c < t.cols);
-            const uint64_t d = t.dst + (uint64_t)((long long)c * t.dst_ld);
-            const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+            const bool colok = col < t.cols;
+            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
             const int d0 = (int)(d & 15u);        // destination phase
             const uint64_t sa = s - (uint64_t)d0; // source byte of chunk 0's first byte
             const int sh = (int)(sa & 15u);       // source phase vs. destination
-            const int rel = (kl + kit * step) << 4;
+            const int rel = k << 4;
             const int lo_lim = sh + d0, hi_lim = sh + d0 + L;
             const bool need = colok && rel < hi_lim && rel + 16 > lo_lim;
             lo[u] = need ? ldg_v4(sa - (uint64_t)sh + (uint64_t)rel)
                          : make_uint4(0u, 0u, 0u, 0u);
+            if (u == U - 1 && !aligned) { // the last lane's next block, from no lane
+                const bool nx = colok && lane == 31 && sh != 0 && rel + 16 < hi_lim;
+                ex = nx ? ldg_v4(sa - (uint64_t)sh + (uint64_t)(rel + 16))
+                        : make_uint4(0u, 0u, 0u, 0u);
+            }
             // words of this chunk inside the destination column [d0, d0 + L)
             int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
             wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
             whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
             uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
-            m = (colok && stores) ? m : 0u;
+            m = colok ? m : 0u;
             chunk[u] = d - (uint64_t)d0 + (uint64_t)rel;
             qm[u] = m | ((uint32_t)(sh >> 2) << 4);
-            if (++kit == nkit) {
-                kit = 0;
-                ++colit;
+            col += dq;
+            k += dr;
+            if (k >= cpc) {
+                k -= cpc;
+                ++col;
+            }
+        }
+        if (NWARP > 1) {
+            col += sq;
+            k += sr;
+            if (k >= cpc) {
+                k -= cpc;
+                ++col;
             }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             uint4 o = lo[u];
             if (!aligned) { // tile-uniform
+                // lane i takes the block of chunk idx + 1: lane i + 1's, or for
+                // lane 31 lane 0's of the next step (its own extra load last)
+                uint4 v = lo[u];
+                if (u + 1 < U && lane == 0)
+                    v = lo[u + 1];
+                const int srcl = (lane + 1) & 31;
                 uint4 nb;
-                nb.x = __shfl_down_sync(0xffffffffu, lo[u].x, 1);
-                nb.y = __shfl_down_sync(0xffffffffu, lo[u].y, 1);
-                nb.z = __shfl_down_sync(0xffffffffu, lo[u].z, 1);
-                nb.w = __shfl_down_sync(0xffffffffu, lo[u].w, 1);
-                const uint32_t q = qm[u] >> 4;
+                nb.x = __shfl_sync(0xffffffffu, v.x, srcl);
+                nb.y = __shfl_sync(0xffffffffu, v.y, srcl);
+                nb.z = __shfl_sync(0xffffffffu, v.z, srcl);
+                nb.w = __shfl_sync(0xffffffffu, v.w, srcl);
+                if (u == U - 1 && lane == 31)
+                    nb = ex;
+                const uint32_t q = (qm[u] >> 4) & 3u;
                 if (q)
                     o = funnel_words(lo[u], nb, q);
             }
@@ -795,9 +824,8 @@ __device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *p
 // register cost of the scaled complex arithmetic.
 enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
 
-// Resident threads per SM: 1024 (64 registers each) for shallow unrolling,
-// 512 (up to 128 registers) for U >= 4, so every variant keeps
-// U x 16 B x threads >= 32 KB of reads in flight per SM without spilling.
+// Register budget: 64 per thread (1024 resident threads per SM), enough for
+// U = 4 chunks per lane in flight on the register path without spilling.
 template <int U, int THREADS> struct MinBlocks {
     static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
 };
@@ -877,6 +905,249 @@ __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
     // phase 2: transposed and scaled tiles, one CTA per tile
     if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
         cta_phase<THREADS, PATHS>(list, smem, td);
+}
+
+// ------------------------------------------------------ cp.async copy ring
+// Phase 1 of the ring kernel: the plain copy tiles of a warp form one stream
+// of stages of 32 x U chunks (the chunk sequence of copy_tile, cut into
+// stages; a stage belongs to one tile). The warp keeps RING_D - 1 stages in
+// flight as cp.async 16-byte copies into a per-warp ring in shared memory,
+// so the reads in flight are bounded by shared memory, not by registers, and
+// continue across tile boundaries. A stage is then stored from shared memory:
+// chunk i of a stage reads its source blocks at ring slots i and i + 1 (slot
+// 32U holds the block after the stage's last chunk, loaded by lane 31).
+// Every wait is cp.async.wait_group, which completes with the copies.
+#ifndef G2G_RING_D
+#define G2G_RING_D 4
+#endif
+constexpr int RING_D = G2G_RING_D; // stages per warp ring (RING_D - 1 in flight)
+
+struct RingRec {        // one stage: its tile, first chunk, chunks per column
+    Tile t;             // 48 B
+    int idx0;           // -1: no stage
+    int cpc;
+    int pad[2];
+};
+static_assert(sizeof(RingRec) == 64, "RingRec is 64 bytes");
+
+template <int U> __host__ __device__ constexpr int ring_warp_bytes() {
+    return RING_D * (U * 32 + 1) * 16 + RING_D * (int)sizeof(RingRec);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gaddr)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// a ring read, ordered after the wait and warp barrier that make it valid
+__device__ __forceinline__ uint4 lds_ring(uint32_t a) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(a)
+                 : "memory");
+    return v;
+}
+
+// chunks per column of a copy tile (as in copy_tile)
+__device__ __forceinline__ int copy_cpc(const Tile &t) {
+    const int L = t.rows * kind_esz(t.kind);
+    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    if (((t.dst_ld | t.src_ld) & 15) == 0) {
+        const int d0 = (int)(t.dst & 15u);
+        const int sh = (int)((t.src - (uint64_t)d0) & 15u);
+        return (sh + d0 + L + 15) >> 4;
+    }
+    return aligned ? ((L + 27) >> 4) : ((L + 39) >> 4);
+}
+
+// Issues the cp.async copies of one stage (chunks idx0 .. idx0 + 32U - 1 of t)
+// into ring slots `slots` (32U + 1 blocks).
+template <int U>
+__device__ __forceinline__ void ring_issue(const Tile &t, int cpc, int idx0, uint32_t slots,
+                                           int lane) {
+    const int L = t.rows * kind_esz(t.kind);
+    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    const int idx = idx0 + lane;
+    int col = idx / cpc, k = idx - (idx / cpc) * cpc;
+    const int dq = 32 / cpc, dr = 32 - dq * cpc;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (col < t.cols) {
+            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
+            const int d0 = (int)(d & 15u);
+            const uint64_t sa = s - (uint64_t)d0;
+            const int sh = (int)(sa & 15u);
+            const int rel = k << 4;
+            const int lo_lim = sh + d0, hi_lim = sh + d0 + L;
+            const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+            if (rel < hi_lim && rel + 16 > lo_lim)
+                cp_async16(slot, sa - (uint64_t)sh + (uint64_t)rel);
+            if (u == U - 1 && lane == 31 && !aligned && sh != 0 && rel + 16 < hi_lim)
+                cp_async16(slot + 16, sa - (uint64_t)sh + (uint64_t)(rel + 16));
+        }
+        col += dq;
+        k += dr;
+        if (k >= cpc) {
+            k -= cpc;
+            ++col;
+        }
+    }
+}
+
+// Stores one landed stage from its ring slots.
+template <int U>
+__device__ __forceinline__ void ring_store(const RingRec &r, uint32_t slots, int lane) {
+    const Tile &t = r.t;
+    const int cpc = r.cpc;
+    const int L = t.rows * kind_esz(t.kind);
+    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    const int idx = r.idx0 + lane;
+    int col = idx / cpc, k = idx - (idx / cpc) * cpc;
+    const int dq = 32 / cpc, dr = 32 - dq * cpc;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (col < t.cols) {
+            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
+            const int d0 = (int)(d & 15u);
+            const int sh = (int)((s - (uint64_t)d0) & 15u);
+            const int rel = k << 4;
+            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
+            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
+            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
+            const uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
+            if (m) {
+                const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+                uint4 o = lds_ring(slot);
+                if (!aligned && sh != 0)
+                    o = funnel_words(o, lds_ring(slot + 16), (uint32_t)(sh >> 2));
+                const uint64_t chunk = d - (uint64_t)d0 + (uint64_t)rel;
+                if (m == 0xFu) {
+                    st_v4(chunk, o);
+                } else {
+                    if (m & 1u) st_u32(chunk, o.x);
+                    if (m & 2u) st_u32(chunk + 4, o.y);
+                    if (m & 4u) st_u32(chunk + 8, o.z);
+                    if (m & 8u) st_u32(chunk + 12, o.w);
+                }
+            }
+        }
+        col += dq;
+        k += dr;
+        if (k >= cpc) {
+            k -= cpc;
+            ++col;
+        }
+    }
+}
+
+// The warp's issue cursor: the tile it is in, that tile's chunk count, the
+// next chunk, and the descriptor of the warp's following tile (loaded ahead).
+struct RingCursor {
+    long long ti;
+    Tile t, nt;
+    int cpc, total, idx0;
+};
+
+__device__ __forceinline__ void ring_load_tile(const PlanList &list, long long ti, Tile &t) {
+    if (ti < list.total_copy) {
+        const PairInfo *unused;
+        t = *locate_copy(list, ti, unused);
+    }
+}
+
+template <int U>
+__device__ __forceinline__ void ring_advance_tile(const PlanList &list, RingCursor &c,
+                                                  long long GW) {
+    c.ti += GW;
+    c.t = c.nt;
+    c.idx0 = 0;
+    if (c.ti < list.total_copy) {
+        c.cpc = copy_cpc(c.t);
+        c.total = c.t.cols * c.cpc;
+        ring_load_tile(list, c.ti + GW, c.nt);
+        if (c.ti + 2 * GW < list.total_copy && (threadIdx.x & 31) == 0) {
+            const PairInfo *unused;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, c.ti + 2 * GW,
+                                                                       unused)));
+        }
+    }
+}
+
+// Fills ring stage `st` from the cursor (or marks it empty) and commits it.
+template <int U>
+__device__ __forceinline__ void ring_fill(const PlanList &list, RingCursor &c, long long GW,
+                                          unsigned char *wbase, int st, int lane) {
+    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * (U * 32 + 1) * 16);
+    const uint32_t slots = smem_addr(wbase) + (uint32_t)(st * (U * 32 + 1) * 16);
+    if (c.ti < list.total_copy) {
+        if (lane == 0) {
+            recs[st].t = c.t;
+            recs[st].idx0 = c.idx0;
+            recs[st].cpc = c.cpc;
+        }
+        ring_issue<U>(c.t, c.cpc, c.idx0, slots, lane);
+        c.idx0 += 32 * U;
+        if (c.idx0 >= c.total)
+            ring_advance_tile<U>(list, c, GW);
+    } else if (lane == 0) {
+        recs[st].idx0 = -1;
+    }
+    cp_async_commit();
+}
+
+template <int U>
+__device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
+                                                int warp, int nwarp) {
+    const int lane = threadIdx.x & 31;
+    unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
+    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * (U * 32 + 1) * 16);
+    const long long GW = (long long)gridDim.x * nwarp;
+    RingCursor c;
+    c.ti = (long long)blockIdx.x * nwarp + warp;
+    c.idx0 = 0;
+    c.cpc = 1;
+    c.total = 0;
+    ring_load_tile(list, c.ti, c.t);
+    ring_load_tile(list, c.ti + GW, c.nt);
+    if (c.ti < list.total_copy) {
+        c.cpc = copy_cpc(c.t);
+        c.total = c.t.cols * c.cpc;
+    }
+#pragma unroll
+    for (int st = 0; st < RING_D - 1; ++st)
+        ring_fill<U>(list, c, GW, wbase, st, lane);
+    int sp = 0; // stage to store; stage RING_D - 1 is filled next
+    for (;;) {
+        ring_fill<U>(list, c, GW, wbase, sp == 0 ? RING_D - 1 : sp - 1, lane);
+        cp_async_wait<RING_D - 1>();
+        __syncwarp();
+        if (recs[sp].idx0 < 0) // stages are filled in order: nothing after this
+            break;
+        ring_store<U>(recs[sp], smem_addr(wbase) + (uint32_t)(sp * (U * 32 + 1) * 16), lane);
+        __syncwarp();
+        sp = sp + 1 == RING_D ? 0 : sp + 1;
+    }
+    cp_async_wait<0>();
+}
+
+template <int THREADS, int U, int PATHS>
+__global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
+    scatter_ring_kernel(const __grid_constant__ PlanList list, int td) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int NWARP = THREADS / 32;
+    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP);
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
+        __syncthreads(); // the ring's shared memory becomes the CTA tiles'
+        cta_phase<THREADS, PATHS>(list, smem, td);
+    }
 }
 
 // The staged variant: a ring of S shared-memory stages filled by TMA bulk
@@ -979,7 +1250,21 @@ cudaError_t launch_staged(const PlanList &list, const ScatterConfig &cfg, cudaSt
 }
 
 template <int THREADS, int U, int PATHS>
+cudaError_t launch_ring(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
+    auto k = scatter_ring_kernel<THREADS, U, PATHS>;
+    const size_t smem = ring_smem_bytes(cfg);
+    unsigned grid = 0;
+    cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim);
+    return cudaGetLastError();
+}
+
+template <int THREADS, int U, int PATHS>
 cudaError_t launch_t(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
+    if ((PATHS & PATH_COPY) && cfg.ring && cfg.stages < 2)
+        return launch_ring<THREADS, U, PATHS>(list, cfg, s);
     if ((PATHS & PATH_COPY) && cfg.stages >= 2) {
         switch (cfg.stages) {
         case 2: return launch_staged<THREADS, U, PATHS, 2>(list, cfg, s);
@@ -1025,6 +1310,14 @@ size_t transpose_smem_bytes(int tile_dim, int esz) {
 int stage_bytes_for(int tile_bytes) {
     const long long b = (long long)tile_bytes * 9 / 8 + 512;
     return (int)((b + 127) / 128 * 128);
+}
+
+size_t ring_smem_bytes(const ScatterConfig &cfg) {
+    const int u = cfg.unroll == 1 ? 1 : (cfg.unroll == 2 ? 2 : 4);
+    const size_t ring = (size_t)(cfg.threads / 32) *
+                        (size_t)(u == 1 ? ring_warp_bytes<1>()
+                                        : (u == 2 ? ring_warp_bytes<2>() : ring_warp_bytes<4>()));
+    return ring > cfg.trans_bytes ? ring : cfg.trans_bytes;
 }
 
 size_t staged_smem_bytes(const ScatterConfig &cfg) {

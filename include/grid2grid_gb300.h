@@ -125,10 +125,13 @@ typedef struct g2g_tuning {
     int32_t ctas_per_sm;      /* persistent grid = ctas_per_sm x SM count   */
     int32_t threads;          /* threads per CTA: 128, 256 or 512           */
     int32_t unroll;           /* 16-byte chunks in flight per thread: 1,2,4,8 */
-    int32_t stages;           /* plain copies: -1 = loads through registers,
+    int32_t stages;           /* plain copies: -1 = not TMA-staged,
                                  2..4 = TMA bulk copies into a ring of that
                                  many shared-memory stages (0 = default)    */
-    int32_t reserved[2];
+    int32_t ring;             /* plain copies when not TMA-staged: 1 = per-warp
+                                 cp.async ring in shared memory, -1 = loads
+                                 through registers (0 = default)            */
+    int32_t reserved;
 } g2g_tuning;
 
 typedef struct g2g_plan_info {

@@ -166,7 +166,10 @@ def test_mixed_dtype_batch_matches_port():
 @pytest.mark.parametrize("tuning", [
     dict(threads=256, unroll=1, stages=-1), dict(threads=256, unroll=2, stages=2), dict(threads=512, unroll=4, stages=4),
     dict(threads=512, unroll=4, stages=-1), dict(tile_bytes=4096, tile_dim=16, stages=3),
-    dict(tile_bytes=65536, tile_dim=32, ctas_per_sm=1, threads=512)])
+    dict(tile_bytes=65536, tile_dim=32, ctas_per_sm=1, threads=512),
+    dict(threads=256, unroll=1, ring=-1), dict(threads=512, unroll=4, ring=-1),
+    dict(threads=256, unroll=2, ring=1), dict(threads=512, unroll=1, ring=1),
+    dict(tile_bytes=512, unroll=4, ring=1, ctas_per_sm=1)])
 def test_tunings_give_identical_results(tuning):
     rng = np.random.default_rng(77)
     inits, finals, ias, fas, ops = [], [], [], [], []
