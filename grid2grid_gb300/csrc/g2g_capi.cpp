@@ -776,9 +776,10 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
         return st;
     }
     // Launch shape by the tiles the plan holds. Plain copies run best as 16
-    // warps per SM, each with its cp.async ring (3 stages of 2 KB in flight):
-    // more concurrent column streams lose DRAM locality. With CTA-level tiles
-    // as well, 256-thread CTAs keep more of those in flight.
+    // warps per SM, each with its cp.async ring (a 2 KB stage in flight while
+    // the previous one is stored): more concurrent column streams lose DRAM
+    // locality. With CTA-level tiles as well, 256-thread CTAs keep more of
+    // those in flight.
     if (pl->n_copy > 0) {
         const bool cta_tiles = pl->n_tiles > pl->n_copy;
         pl->tuning.threads = cta_tiles ? 256 : 512;

@@ -911,22 +911,26 @@ __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
 // Phase 1 of the ring kernel: the plain copy tiles of a warp form one stream
 // of stages of 32 x U chunks (the chunk sequence of copy_tile, cut into
 // stages; a stage belongs to one tile). The warp keeps RING_D - 1 stages in
-// flight as cp.async 16-byte copies into a per-warp ring in shared memory,
-// so the reads in flight are bounded by shared memory, not by registers, and
-// continue across tile boundaries. A stage is then stored from shared memory:
+// flight as cp.async 16-byte copies into a per-warp ring in shared memory
+// while it stores the oldest landed stage, so its reads continue across tile
+// boundaries and overlap its own stores. Two stages (one in flight while one
+// is stored) at 16 warps per SM measured best on the layouts tried: deeper
+// rings or more warps put more concurrent column streams on the DRAM and
+// lose row locality. A stage is then stored from shared memory:
 // chunk i of a stage reads its source blocks at ring slots i and i + 1 (slot
 // 32U holds the block after the stage's last chunk, loaded by lane 31).
+// The issuing and the storing side each walk the chunk sequence with their
+// own cursor (column, chunk, column addresses), advanced by additions only.
 // Every wait is cp.async.wait_group, which completes with the copies.
 #ifndef G2G_RING_D
-#define G2G_RING_D 4
+#define G2G_RING_D 2
 #endif
 constexpr int RING_D = G2G_RING_D; // stages per warp ring (RING_D - 1 in flight)
 
-struct RingRec {        // one stage: its tile, first chunk, chunks per column
-    Tile t;             // 48 B
-    int idx0;           // -1: no stage
-    int cpc;
-    int pad[2];
+struct RingRec {        // one stage
+    Tile t;             // the tile, written for a tile's first stage only
+    int valid;          // 0: no stage (the warp's work is done)
+    int pad[3];
 };
 static_assert(sizeof(RingRec) == 64, "RingRec is 64 bytes");
 
@@ -954,107 +958,117 @@ __device__ __forceinline__ uint4 lds_ring(uint32_t a) {
     return v;
 }
 
-// chunks per column of a copy tile (as in copy_tile)
-__device__ __forceinline__ int copy_cpc(const Tile &t) {
-    const int L = t.rows * kind_esz(t.kind);
-    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+// Per-tile constants of a chunk walk (chunks per column as in copy_tile).
+struct RingTile {
+    uint64_t dst, src;
+    long long dld, sld;     // column strides, bytes
+    long long stepd, steps; // dq columns, bytes
+    int cols, L, cpc, dq, dr, total;
+    bool aligned;
+};
+__device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
+    c.dst = t.dst;
+    c.src = t.src;
+    c.dld = t.dst_ld;
+    c.sld = t.src_ld;
+    c.cols = t.cols;
+    c.L = t.rows * kind_esz(t.kind);
+    c.aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
     if (((t.dst_ld | t.src_ld) & 15) == 0) {
         const int d0 = (int)(t.dst & 15u);
         const int sh = (int)((t.src - (uint64_t)d0) & 15u);
-        return (sh + d0 + L + 15) >> 4;
+        c.cpc = (sh + d0 + c.L + 15) >> 4;
+    } else {
+        c.cpc = c.aligned ? ((c.L + 27) >> 4) : ((c.L + 39) >> 4);
     }
-    return aligned ? ((L + 27) >> 4) : ((L + 39) >> 4);
+    c.dq = 32 / c.cpc;
+    c.dr = 32 - c.dq * c.cpc;
+    c.stepd = (long long)c.dq * c.dld;
+    c.steps = (long long)c.dq * c.sld;
+    c.total = c.cols * c.cpc;
 }
 
-// Issues the cp.async copies of one stage (chunks idx0 .. idx0 + 32U - 1 of t)
-// into ring slots `slots` (32U + 1 blocks).
+// A lane's position: chunk k of column col, whose addresses are d / s.
+struct RingWalk {
+    uint64_t d, s;
+    int col, k;
+};
+__device__ __forceinline__ void ring_walk_init(RingWalk &w, const RingTile &c, int idx) {
+    w.col = idx / c.cpc;
+    w.k = idx - w.col * c.cpc;
+    w.d = c.dst + (uint64_t)((long long)w.col * c.dld);
+    w.s = c.src + (uint64_t)((long long)w.col * c.sld);
+}
+__device__ __forceinline__ void ring_walk_step(RingWalk &w, const RingTile &c) { // +32 chunks
+    w.col += c.dq;
+    w.k += c.dr;
+    w.d += (uint64_t)c.stepd;
+    w.s += (uint64_t)c.steps;
+    if (w.k >= c.cpc) {
+        w.k -= c.cpc;
+        ++w.col;
+        w.d += (uint64_t)c.dld;
+        w.s += (uint64_t)c.sld;
+    }
+}
+
+// Issues the cp.async copies of one stage into ring slots `slots`.
 template <int U>
-__device__ __forceinline__ void ring_issue(const Tile &t, int cpc, int idx0, uint32_t slots,
+__device__ __forceinline__ void ring_issue(const RingTile &c, RingWalk &w, uint32_t slots,
                                            int lane) {
-    const int L = t.rows * kind_esz(t.kind);
-    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
-    const int idx = idx0 + lane;
-    int col = idx / cpc, k = idx - (idx / cpc) * cpc;
-    const int dq = 32 / cpc, dr = 32 - dq * cpc;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        if (col < t.cols) {
-            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
-            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
-            const int d0 = (int)(d & 15u);
-            const uint64_t sa = s - (uint64_t)d0;
+        if (w.col < c.cols) {
+            const int d0 = (int)(w.d & 15u);
+            const uint64_t sa = w.s - (uint64_t)d0; // source byte under chunk 0's first byte
             const int sh = (int)(sa & 15u);
-            const int rel = k << 4;
-            const int lo_lim = sh + d0, hi_lim = sh + d0 + L;
+            const uint64_t base = sa - (uint64_t)sh;
+            const int rel = w.k << 4;
+            const int lo = sh + d0, hi = sh + d0 + c.L;
             const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
-            if (rel < hi_lim && rel + 16 > lo_lim)
-                cp_async16(slot, sa - (uint64_t)sh + (uint64_t)rel);
-            if (u == U - 1 && lane == 31 && !aligned && sh != 0 && rel + 16 < hi_lim)
-                cp_async16(slot + 16, sa - (uint64_t)sh + (uint64_t)(rel + 16));
+            if (rel < hi && rel + 16 > lo)
+                cp_async16(slot, base + (uint64_t)rel);
+            if (u == U - 1 && lane == 31 && sh != 0 && rel + 16 < hi)
+                cp_async16(slot + 16, base + (uint64_t)(rel + 16));
         }
-        col += dq;
-        k += dr;
-        if (k >= cpc) {
-            k -= cpc;
-            ++col;
-        }
+        ring_walk_step(w, c);
     }
 }
 
 // Stores one landed stage from its ring slots.
 template <int U>
-__device__ __forceinline__ void ring_store(const RingRec &r, uint32_t slots, int lane) {
-    const Tile &t = r.t;
-    const int cpc = r.cpc;
-    const int L = t.rows * kind_esz(t.kind);
-    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
-    const int idx = r.idx0 + lane;
-    int col = idx / cpc, k = idx - (idx / cpc) * cpc;
-    const int dq = 32 / cpc, dr = 32 - dq * cpc;
+__device__ __forceinline__ void ring_store(const RingTile &c, RingWalk &w, uint32_t slots,
+                                           int lane) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        if (col < t.cols) {
-            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
-            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
-            const int d0 = (int)(d & 15u);
-            const int sh = (int)((s - (uint64_t)d0) & 15u);
-            const int rel = k << 4;
-            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
-            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
-            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
-            const uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
-            if (m) {
+        if (w.col < c.cols) {
+            const int d0 = (int)(w.d & 15u);
+            const int rel = w.k << 4;
+            const int end = d0 + c.L;
+            if (rel + 16 > d0 && rel < end) { // the chunk holds destination words
                 const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
                 uint4 o = lds_ring(slot);
-                if (!aligned && sh != 0)
-                    o = funnel_words(o, lds_ring(slot + 16), (uint32_t)(sh >> 2));
-                const uint64_t chunk = d - (uint64_t)d0 + (uint64_t)rel;
-                if (m == 0xFu) {
+                if (!c.aligned) {
+                    const int sh = (int)((w.s - (uint64_t)d0) & 15u);
+                    if (sh)
+                        o = funnel_words(o, lds_ring(slot + 16), (uint32_t)(sh >> 2));
+                }
+                const uint64_t chunk = w.d - (uint64_t)d0 + (uint64_t)rel;
+                if (rel >= d0 && rel + 16 <= end) {
                     st_v4(chunk, o);
-                } else {
-                    if (m & 1u) st_u32(chunk, o.x);
-                    if (m & 2u) st_u32(chunk + 4, o.y);
-                    if (m & 4u) st_u32(chunk + 8, o.z);
-                    if (m & 8u) st_u32(chunk + 12, o.w);
+                } else { // head or tail chunk of the column: whole words
+                    const int wlo = rel >= d0 ? 0 : (d0 - rel) >> 2;
+                    const int whi = rel + 16 <= end ? 4 : (end - rel) >> 2;
+                    if (wlo <= 0 && whi > 0) st_u32(chunk, o.x);
+                    if (wlo <= 1 && whi > 1) st_u32(chunk + 4, o.y);
+                    if (wlo <= 2 && whi > 2) st_u32(chunk + 8, o.z);
+                    if (wlo <= 3 && whi > 3) st_u32(chunk + 12, o.w);
                 }
             }
         }
-        col += dq;
-        k += dr;
-        if (k >= cpc) {
-            k -= cpc;
-            ++col;
-        }
+        ring_walk_step(w, c);
     }
 }
-
-// The warp's issue cursor: the tile it is in, that tile's chunk count, the
-// next chunk, and the descriptor of the warp's following tile (loaded ahead).
-struct RingCursor {
-    long long ti;
-    Tile t, nt;
-    int cpc, total, idx0;
-};
 
 __device__ __forceinline__ void ring_load_tile(const PlanList &list, long long ti, Tile &t) {
     if (ti < list.total_copy) {
@@ -1063,42 +1077,45 @@ __device__ __forceinline__ void ring_load_tile(const PlanList &list, long long t
     }
 }
 
-template <int U>
-__device__ __forceinline__ void ring_advance_tile(const PlanList &list, RingCursor &c,
-                                                  long long GW) {
-    c.ti += GW;
-    c.t = c.nt;
-    c.idx0 = 0;
-    if (c.ti < list.total_copy) {
-        c.cpc = copy_cpc(c.t);
-        c.total = c.t.cols * c.cpc;
-        ring_load_tile(list, c.ti + GW, c.nt);
-        if (c.ti + 2 * GW < list.total_copy && (threadIdx.x & 31) == 0) {
-            const PairInfo *unused;
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, c.ti + 2 * GW,
-                                                                       unused)));
-        }
-    }
-}
+// The issuing side: the tile it is in (its descriptor until its first stage
+// is recorded), its walk, and the descriptor of the warp's next tile.
+struct RingIssue {
+    long long ti;
+    Tile cur, nt;
+    RingTile c;
+    RingWalk w;
+    int idx0;
+};
 
-// Fills ring stage `st` from the cursor (or marks it empty) and commits it.
+// Fills ring stage `st` from the issuing cursor (or marks it empty) and commits it.
 template <int U>
-__device__ __forceinline__ void ring_fill(const PlanList &list, RingCursor &c, long long GW,
-                                          unsigned char *wbase, int st, int lane) {
-    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * (U * 32 + 1) * 16);
-    const uint32_t slots = smem_addr(wbase) + (uint32_t)(st * (U * 32 + 1) * 16);
-    if (c.ti < list.total_copy) {
+__device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q, long long GW,
+                                          uint32_t slots, RingRec &rec, int lane) {
+    if (q.ti < list.total_copy) {
         if (lane == 0) {
-            recs[st].t = c.t;
-            recs[st].idx0 = c.idx0;
-            recs[st].cpc = c.cpc;
+            if (q.idx0 == 0)
+                rec.t = q.cur;
+            rec.valid = 1;
         }
-        ring_issue<U>(c.t, c.cpc, c.idx0, slots, lane);
-        c.idx0 += 32 * U;
-        if (c.idx0 >= c.total)
-            ring_advance_tile<U>(list, c, GW);
+        ring_issue<U>(q.c, q.w, slots, lane);
+        q.idx0 += 32 * U;
+        if (q.idx0 >= q.c.total) { // on to the warp's next tile
+            q.ti += GW;
+            q.idx0 = 0;
+            if (q.ti < list.total_copy) {
+                q.cur = q.nt;
+                ring_tile_init(q.c, q.cur);
+                ring_walk_init(q.w, q.c, lane);
+                ring_load_tile(list, q.ti + GW, q.nt);
+                if (lane == 0 && q.ti + 2 * GW < list.total_copy) {
+                    const PairInfo *unused;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(
+                        locate_copy(list, q.ti + 2 * GW, unused)));
+                }
+            }
+        }
     } else if (lane == 0) {
-        recs[st].idx0 = -1;
+        rec.valid = 0;
     }
     cp_async_commit();
 }
@@ -1106,40 +1123,58 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingCursor &c, l
 template <int U>
 __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
                                                 int warp, int nwarp) {
+    constexpr int SLOT_BYTES = (U * 32 + 1) * 16;
     const int lane = threadIdx.x & 31;
     unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
-    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * (U * 32 + 1) * 16);
+    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * SLOT_BYTES);
+    const uint32_t slots0 = smem_addr(wbase);
     const long long GW = (long long)gridDim.x * nwarp;
-    RingCursor c;
-    c.ti = (long long)blockIdx.x * nwarp + warp;
-    c.idx0 = 0;
-    c.cpc = 1;
-    c.total = 0;
-    ring_load_tile(list, c.ti, c.t);
-    ring_load_tile(list, c.ti + GW, c.nt);
-    if (c.ti < list.total_copy) {
-        c.cpc = copy_cpc(c.t);
-        c.total = c.t.cols * c.cpc;
+    RingIssue q;
+    q.ti = (long long)blockIdx.x * nwarp + warp;
+    q.idx0 = 0;
+    ring_load_tile(list, q.ti, q.cur);
+    ring_load_tile(list, q.ti + GW, q.nt);
+    if (q.ti < list.total_copy) {
+        ring_tile_init(q.c, q.cur);
+        ring_walk_init(q.w, q.c, lane);
     }
 #pragma unroll
     for (int st = 0; st < RING_D - 1; ++st)
-        ring_fill<U>(list, c, GW, wbase, st, lane);
-    int sp = 0; // stage to store; stage RING_D - 1 is filled next
+        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(st * SLOT_BYTES), recs[st], lane);
+    // the storing side
+    RingTile c;
+    RingWalk w;
+    int idx0 = 0;
+    c.total = 0;
+    int sp = 0; // stage to store; the stage before it is filled next
     for (;;) {
-        ring_fill<U>(list, c, GW, wbase, sp == 0 ? RING_D - 1 : sp - 1, lane);
+        const int sf = sp == 0 ? RING_D - 1 : sp - 1;
+        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(sf * SLOT_BYTES), recs[sf], lane);
         cp_async_wait<RING_D - 1>();
         __syncwarp();
-        if (recs[sp].idx0 < 0) // stages are filled in order: nothing after this
+        if (!recs[sp].valid) // stages are filled in order: nothing after this
             break;
-        ring_store<U>(recs[sp], smem_addr(wbase) + (uint32_t)(sp * (U * 32 + 1) * 16), lane);
+        if (idx0 >= c.total) { // the stage starts the next tile
+            ring_tile_init(c, recs[sp].t);
+            ring_walk_init(w, c, lane);
+            idx0 = 0;
+        }
+        ring_store<U>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES), lane);
+        idx0 += 32 * U;
         __syncwarp();
         sp = sp + 1 == RING_D ? 0 : sp + 1;
     }
     cp_async_wait<0>();
 }
 
+// Registers: the ring kernel runs 16 warps per SM on copy-only plans (one
+// 512-thread CTA, or two of 256), 24 with CTA-level tiles (three of 256).
+template <int THREADS> struct RingMinBlocks {
+    static constexpr int value = (768 / THREADS) > 0 ? (768 / THREADS) : 1;
+};
+
 template <int THREADS, int U, int PATHS>
-__global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
+__global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS>::value))
     scatter_ring_kernel(const __grid_constant__ PlanList list, int td) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;

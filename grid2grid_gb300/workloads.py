@@ -133,4 +133,5 @@ BY_NAME = {
     "random_grid_f32_16384": random_grid_f32_16384,
     "transposed_c128_8192": transposed_c128_8192,
     "uneven_batch_256": uneven_batch,
+    "uneven_batch_64": lambda: uneven_batch(64),
 }
