@@ -751,61 +751,112 @@ __device__ __forceinline__ bool is_plain_transpose(const Tile &t) {
     return (t.kind & KIND_TRANS) && !(t.kind & KIND_SCALED);
 }
 
-// Element i of this thread in a td x td tile (td a power of two): load view
-// (storage column r = final row, contiguous along c = final column).
-template <int THREADS, int NE>
-__device__ __forceinline__ void load_tile_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
-    const int td = 1 << td_shift;
-    const int mode = elem_mode(t);
-    const int esz = kind_esz(t.kind);
+// A td x td tile (td a power of two) over a CTA: thread x owns one lane of
+// the tile's contiguous direction and every (THREADS / td)-th line of the
+// other, so its addresses advance by a constant step. The element mode is
+// uniform per tile and a template argument here, so no access branches on it.
+template <int MODE> struct ModeEsz {
+    static constexpr int value = MODE == EM_4 ? 4 : (MODE <= EM_8_SPLIT ? 8 : 16);
+};
+
+// Load view: line r = storage column of the source (= final row), lane c
+// along it (= final column).
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void load_slots_m(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    const int c = threadIdx.x & ((1 << td_shift) - 1);
+    const int r0 = threadIdx.x >> td_shift;
+    const int rstep = THREADS >> td_shift;
+    if (c >= t.cols)
+        return;
+    uint64_t a = t.src + (uint64_t)((long long)r0 * t.src_ld + (long long)c * ESZ);
+    const uint64_t step = (uint64_t)((long long)rstep * t.src_ld);
 #pragma unroll
     for (int i = 0; i < NE; ++i) {
-        const int idx = threadIdx.x + i * THREADS;
-        const int r = idx >> td_shift, c = idx & (td - 1);
-        if (idx < (td << td_shift) && r < t.rows && c < t.cols)
-            v[i] = ld_elem_raw(t.src + (uint64_t)((long long)r * t.src_ld + (long long)c * esz),
-                               mode);
+        if (r0 + i * rstep < t.rows)
+            v[i] = ld_elem_raw(a, MODE);
+        a += step;
     }
 }
 
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void slots_to_smem_m(const Tile &t, int td_shift,
+                                                const uint4 (&v)[NE], unsigned char *smem) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    const int td = 1 << td_shift;
+    const int c = threadIdx.x & (td - 1);
+    const int r0 = threadIdx.x >> td_shift;
+    const int rstep = THREADS >> td_shift;
+    if (c >= t.cols)
+        return;
+    unsigned char *p = smem + (size_t)(r0 * (td + 1) + c) * ESZ;
+    const int step = rstep * (td + 1) * ESZ;
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        if (r0 + i * rstep < t.rows)
+            sts_elem(p, v[i], ESZ);
+        p += step;
+    }
+}
+
+// Store view: line c = destination storage column (= final column), lane r
+// along it (= final row).
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void smem_to_global_m(const Tile &t, int td_shift,
+                                                 const unsigned char *smem) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    const int td = 1 << td_shift;
+    const int r = threadIdx.x & (td - 1);
+    const int c0 = threadIdx.x >> td_shift;
+    const int cstep = THREADS >> td_shift;
+    if (r >= t.rows)
+        return;
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    const unsigned char *p = smem + (size_t)(r * (td + 1) + c0) * ESZ;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ESZ);
+    const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        if (c0 + i * cstep < t.cols) {
+            uint4 e = lds_elem(p, ESZ);
+            if (conj) { // sign of the imaginary part: top word of the element
+                if (ESZ == 8)
+                    e.y ^= 0x80000000u;
+                else if (ESZ == 16)
+                    e.w ^= 0x80000000u;
+            }
+            st_elem_raw(a, e, MODE);
+        }
+        p += cstep * ESZ;
+        a += step;
+    }
+}
+
+#define G2G_MODE_DISPATCH(FN, ...)                                                  \
+    switch (elem_mode(t)) {                                                         \
+    case EM_4: FN<THREADS, NE, EM_4>(__VA_ARGS__); break;                           \
+    case EM_8: FN<THREADS, NE, EM_8>(__VA_ARGS__); break;                           \
+    case EM_8_SPLIT: FN<THREADS, NE, EM_8_SPLIT>(__VA_ARGS__); break;               \
+    case EM_16: FN<THREADS, NE, EM_16>(__VA_ARGS__); break;                         \
+    case EM_16_SPLIT8: FN<THREADS, NE, EM_16_SPLIT8>(__VA_ARGS__); break;           \
+    default: FN<THREADS, NE, EM_16_SPLIT4>(__VA_ARGS__); break;                     \
+    }
+
+template <int THREADS, int NE>
+__device__ __forceinline__ void load_tile_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    G2G_MODE_DISPATCH(load_slots_m, t, td_shift, v)
+}
 template <int THREADS, int NE>
 __device__ __forceinline__ void slots_to_smem(const Tile &t, int td_shift, const uint4 (&v)[NE],
                                               unsigned char *smem) {
-    const int td = 1 << td_shift;
-    const int esz = kind_esz(t.kind);
-#pragma unroll
-    for (int i = 0; i < NE; ++i) {
-        const int idx = threadIdx.x + i * THREADS;
-        const int r = idx >> td_shift, c = idx & (td - 1);
-        if (idx < (td << td_shift) && r < t.rows && c < t.cols)
-            sts_elem(smem + (size_t)(r * (td + 1) + c) * esz, v[i], esz);
-    }
+    G2G_MODE_DISPATCH(slots_to_smem_m, t, td_shift, v, smem)
 }
-
-// Store view: destination column c (storage row), contiguous along r.
 template <int THREADS, int NE>
 __device__ __forceinline__ void smem_to_global(const Tile &t, int td_shift,
                                                const unsigned char *smem) {
-    const int td = 1 << td_shift;
-    const int mode = elem_mode(t);
-    const int esz = kind_esz(t.kind);
-    const bool conj = (t.kind & KIND_CONJ) != 0;
-#pragma unroll
-    for (int i = 0; i < NE; ++i) {
-        const int idx = threadIdx.x + i * THREADS;
-        const int c = idx >> td_shift, r = idx & (td - 1);
-        if (idx < (td << td_shift) && r < t.rows && c < t.cols) {
-            uint4 e = lds_elem(smem + (size_t)(r * (td + 1) + c) * esz, esz);
-            if (conj) { // sign of the imaginary part: top word of the element
-                if (esz == 8)
-                    e.y ^= 0x80000000u;
-                else if (esz == 16)
-                    e.w ^= 0x80000000u;
-            }
-            st_elem_raw(t.dst + (uint64_t)((long long)c * t.dst_ld + (long long)r * esz), e, mode);
-        }
-    }
+    G2G_MODE_DISPATCH(smem_to_global_m, t, td_shift, smem)
 }
+#undef G2G_MODE_DISPATCH
 
 // ------------------------------------------------------------------ kernel
 template <int THREADS>
@@ -1298,13 +1349,15 @@ cudaError_t launch_ring(const PlanList &list, const ScatterConfig &cfg, cudaStre
 
 template <int THREADS, int U, int PATHS>
 cudaError_t launch_t(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
-    if ((PATHS & PATH_COPY) && cfg.ring && cfg.stages < 2)
-        return launch_ring<THREADS, U, PATHS>(list, cfg, s);
-    if ((PATHS & PATH_COPY) && cfg.stages >= 2) {
-        switch (cfg.stages) {
-        case 2: return launch_staged<THREADS, U, PATHS, 2>(list, cfg, s);
-        case 3: return launch_staged<THREADS, U, PATHS, 3>(list, cfg, s);
-        default: return launch_staged<THREADS, U, PATHS, 4>(list, cfg, s);
+    if constexpr ((PATHS & PATH_COPY) != 0) {
+        if (cfg.ring && cfg.stages < 2)
+            return launch_ring<THREADS, U, PATHS>(list, cfg, s);
+        if (cfg.stages >= 2) {
+            switch (cfg.stages) {
+            case 2: return launch_staged<THREADS, U, PATHS, 2>(list, cfg, s);
+            case 3: return launch_staged<THREADS, U, PATHS, 3>(list, cfg, s);
+            default: return launch_staged<THREADS, U, PATHS, 4>(list, cfg, s);
+            }
         }
     }
     auto k = scatter_kernel<THREADS, U, PATHS>;
