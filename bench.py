@@ -552,11 +552,21 @@ def run_serving(lib, pool, rates, duration_s, seed=5):
         servers[mode] = srv
     out = {"budget_bytes": 120 * 10**9, "duration_s": duration_s, "rates": {}}
     try:
-        for mode, srv in servers.items():  # warm the plan caches
+        for mode, srv in servers.items():
+            # warm the plan caches (a burst of every pair), then the launch
+            # path at a low rate (0.2 s at the first rate), both discarded
             idx = (C.c_int32 * n)(*range(n))
             arr = (C.c_double * n)(*([0.0] * n))
             times = (capi.RequestTimes * n)()
             capi.check(lib.g2g_server_replay(srv, n, dI, dF, dts, None, n, idx, arr, times))
+            Nw = max(1, int(rates[0] * 0.2))
+            warr = np.cumsum(rng.exponential(1.0 / rates[0], size=Nw)).astype(np.float64)
+            wpick = rng.integers(0, n, size=Nw).astype(np.int32)
+            wtimes = (capi.RequestTimes * Nw)()
+            capi.check(lib.g2g_server_replay(srv, n, dI, dF, dts, None, Nw,
+                                             wpick.ctypes.data_as(C.POINTER(C.c_int32)),
+                                             warr.ctypes.data_as(C.POINTER(C.c_double)),
+                                             wtimes))
         for rate in rates:
             N = int(rate * duration_s)
             arrivals = np.cumsum(rng.exponential(1.0 / rate, size=N))

@@ -78,6 +78,11 @@ int stage_bytes_for(int tile_bytes);
 size_t staged_smem_bytes(const ScatterConfig &cfg);
 // Dynamic shared memory of the ring kernel.
 size_t ring_smem_bytes(const ScatterConfig &cfg);
+// The kernel instances by CTA size (one translation unit each).
+cudaError_t launch_scatter_256(const PlanList &list, const ScatterConfig &cfg,
+                               cudaStream_t stream);
+cudaError_t launch_scatter_512(const PlanList &list, const ScatterConfig &cfg,
+                               cudaStream_t stream);
 
 
 // Shared memory a transposed tile of edge `tile_dim` with elements of `esz`

@@ -1,0 +1,1396 @@
+// The gather-scatter: one persistent kernel that replaces the reference's
+// pack (communication_data.cpp:132-142), MPI exchange (transform.cpp:41-124),
+// local copy (communication_data.cpp:224-252) and unpack
+// (communication_data.cpp:157-173). Every tile of the work list is a
+// sub-rectangle of one piece (initial block x final block); its source is read
+// once and its destination written once, straight from the initial owner's
+// strided block into the final owner's strided block.
+//
+// Three tile paths (uniform per tile, so no divergence):
+//  * plain copies    non-transposed: byte movement in 16-byte chunks aligned
+//                    to the DESTINATION, the chunks of a tile's columns walked
+//                    as one flat sequence by the lanes of a warp. When source
+//                    and destination are misaligned differently (arbitrary
+//                    strides), a chunk is assembled from two aligned source
+//                    blocks, funnel-shifted by whole words. Loads and stores
+//                    are 128-bit; only the head and tail chunk of a column
+//                    store single words (memory_utils.hpp:41-77). Two forms:
+//                    the source blocks staged by cp.async in a per-warp ring
+//                    in shared memory (ring kernel, default), or held in
+//                    registers (copy_tile).
+//  * transposed      plain, transposed (+ conjugated): a tile staged through
+//                    shared memory with a padded pitch, loaded coalesced along
+//                    the source's storage columns and stored coalesced along
+//                    the destination's columns, the next tile's loads issued
+//                    before the current one is stored (memory_utils.hpp:124-184).
+//  * scaled tiles    dst = beta*dst + alpha*op(src) in the element type with
+//                    the rounding of the reference's host arithmetic: every
+//                    product and sum rounded separately, complex products in
+//                    the C99 Annex G form that GCC's std::complex multiply uses
+//                    (memory_utils.hpp:25-39,79-122,186-256).
+#pragma once
+
+#include "g2g_internal.hpp"
+#include "g2g_launch.hpp"
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace g2g {
+
+namespace {
+
+// ---------------------------------------------------------------- memory ops
+__device__ __forceinline__ uint4 ldg_v4(uint64_t addr) {
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(addr));
+    return v;
+}
+
+__device__ __forceinline__ void st_v4(uint64_t addr, uint4 v) {
+    asm volatile("st.global.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(addr), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ void st_u32(uint64_t addr, uint32_t v) {
+    asm volatile("st.global.u32 [%0], %1;" ::"l"(addr), "r"(v) : "memory");
+}
+
+template <typename W> __device__ __forceinline__ W ldg_w(uint64_t addr);
+template <> __device__ __forceinline__ uint32_t ldg_w<uint32_t>(uint64_t a) {
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(a));
+    return v;
+}
+template <> __device__ __forceinline__ unsigned long long ldg_w<unsigned long long>(uint64_t a) {
+    unsigned long long v;
+    asm("ld.global.nc.L1::no_allocate.u64 %0, [%1];" : "=l"(v) : "l"(a));
+    return v;
+}
+template <> __device__ __forceinline__ uint4 ldg_w<uint4>(uint64_t a) { return ldg_v4(a); }
+
+template <typename W> __device__ __forceinline__ void st_w(uint64_t addr, W v);
+template <> __device__ __forceinline__ void st_w<uint32_t>(uint64_t a, uint32_t v) {
+    st_u32(a, v);
+}
+template <> __device__ __forceinline__ void st_w<unsigned long long>(uint64_t a,
+                                                                     unsigned long long v) {
+    asm volatile("st.global.u64 [%0], %1;" ::"l"(a), "l"(v) : "memory");
+}
+template <> __device__ __forceinline__ void st_w<uint4>(uint64_t a, uint4 v) { st_v4(a, v); }
+
+// Flip the sign bit of the highest 32-bit word of an element: the sign of the
+// imaginary part of a little-endian std::complex<float|double>, i.e.
+// std::conj (block.cpp:15-21), NaN payloads included.
+__device__ __forceinline__ void flip_top_sign(uint32_t &w) { w ^= 0x80000000u; }
+__device__ __forceinline__ void flip_top_sign(unsigned long long &w) {
+    w ^= 0x8000000000000000ull;
+}
+__device__ __forceinline__ void flip_top_sign(uint4 &w) { w.w ^= 0x80000000u; }
+
+// word-granular funnel: 4 words starting at word q of the 8-word window lo:hi
+__device__ __forceinline__ uint4 funnel_words(uint4 lo, uint4 hi, uint32_t q) {
+    uint32_t a0, a1, a2, a3, a4;
+    if (q & 2u) {
+        a0 = lo.z; a1 = lo.w; a2 = hi.x; a3 = hi.y; a4 = hi.z;
+    } else {
+        a0 = lo.x; a1 = lo.y; a2 = lo.z; a3 = lo.w; a4 = hi.x;
+    }
+    uint4 o;
+    if (q & 1u) {
+        o.x = a1; o.y = a2; o.z = a3; o.w = a4;
+    } else {
+        o.x = a0; o.y = a1; o.z = a2; o.w = a3;
+    }
+    return o;
+}
+
+// ------------------------------------------------------------ plain copy tile
+// The tile's columns are cut into 16-byte chunks aligned to the DESTINATION;
+// the chunks of all columns form one flat sequence (column by column) that the
+// lanes walk 32 at a time, so a warp instruction covers 32 chunks whatever
+// the column length (no lane idles on short columns).
+//  * aligned tiles (source and destination at the same 16-byte phase in every
+//    column): chunk k of a column is one 128-bit load and one 128-bit store;
+//  * otherwise destination chunk k is assembled from aligned source blocks k
+//    and k + 1 (funnel shift by whole words). Lane i loads block k; block
+//    k + 1 is the next chunk of the sequence, loaded by the next lane (warp
+//    shuffle) -- or, past lane 31, by lane 0 of the next unrolled step. Only
+//    the last lane of the last step loads its next block itself. A column is
+//    given as many chunks as aligned source blocks it touches, so its last
+//    chunk never needs the next column's block.
+// A column of a tile is at most 4 KB (tiles are cut at 4096 / sizeof(T)
+// rows), so per-chunk arithmetic is 32-bit, relative to the column's first
+// aligned destination chunk. Only 16-byte blocks overlapping the column are
+// read, so no access leaves the pages the column lives in; stores cover
+// exactly the column (word-masked head and tail chunks).
+// NWARP warps share a tile in runs of 32 * U consecutive chunks.
+template <int NWARP, int U>
+__device__ __forceinline__ void copy_tile(const Tile &t, const int warp) {
+    const int lane = threadIdx.x & 31;
+    const int esz = kind_esz(t.kind);
+    const int L = t.rows * esz; // bytes per column, <= 4096
+    if (L <= 0 || t.cols <= 0)
+        return;
+    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    // chunks per column: the aligned source blocks a column touches from the
+    // block under its first destination chunk (exact when every column has
+    // the same 16-byte phases, else the bound over all phases: element
+    // addresses are 4-byte aligned, so the source lead is at most 24 bytes)
+    int cpc;
+    if (((t.dst_ld | t.src_ld) & 15) == 0) {
+        const int d0 = (int)(t.dst & 15u);
+        const int sh = (int)((t.src - (uint64_t)d0) & 15u);
+        cpc = (sh + d0 + L + 15) >> 4;
+    } else {
+        cpc = aligned ? ((L + 27) >> 4) : ((L + 39) >> 4);
+    }
+    const int total = t.cols * cpc;
+    // flat chunk index of this lane: run r = i * NWARP + warp, idx = r * 32U + u * 32 + lane
+    int col, k;
+    {
+        const int idx = warp * 32 * U + lane;
+        col = idx / cpc;
+        k = idx - col * cpc;
+    }
+    const int dq = 32 / cpc, dr = 32 - dq * cpc;                 // +32 chunks
+    const int skip = (NWARP - 1) * 32 * U;                       // to this warp's next run
+    const int sq = skip / cpc, sr = skip - sq * cpc;
+    for (int base = warp * 32 * U; base < total; base += NWARP * 32 * U) { // warp-uniform
+        uint4 lo[U];
+        uint4 ex;
+        uint64_t chunk[U];
+        uint32_t qm[U]; // bits 0-3 store mask, bits 4-5 word shift
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool colok = col < t.cols;
+            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
+            const int d0 = (int)(d & 15u);        // destination phase
+            const uint64_t sa = s - (uint64_t)d0; // source byte of chunk 0's first byte
+            const int sh = (int)(sa & 15u);       // source phase vs. destination
+            const int rel = k << 4;
+            const int lo_lim = sh + d0, hi_lim = sh + d0 + L;
+            const bool need = colok && rel < hi_lim && rel + 16 > lo_lim;
+            lo[u] = need ? ldg_v4(sa - (uint64_t)sh + (uint64_t)rel)
+                         : make_uint4(0u, 0u, 0u, 0u);
+            if (u == U - 1 && !aligned) { // the last lane's next block, from no lane
+                const bool nx = colok && lane == 31 && sh != 0 && rel + 16 < hi_lim;
+                ex = nx ? ldg_v4(sa - (uint64_t)sh + (uint64_t)(rel + 16))
+                        : make_uint4(0u, 0u, 0u, 0u);
+            }
+            // words of this chunk inside the destination column [d0, d0 + L)
+            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
+            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
+            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
+            uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
+            m = colok ? m : 0u;
+            chunk[u] = d - (uint64_t)d0 + (uint64_t)rel;
+            qm[u] = m | ((uint32_t)(sh >> 2) << 4);
+            col += dq;
+            k += dr;
+            if (k >= cpc) {
+                k -= cpc;
+                ++col;
+            }
+        }
+        if (NWARP > 1) {
+            col += sq;
+            k += sr;
+            if (k >= cpc) {
+                k -= cpc;
+                ++col;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            uint4 o = lo[u];
+            if (!aligned) { // tile-uniform
+                // lane i takes the block of chunk idx + 1: lane i + 1's, or for
+                // lane 31 lane 0's of the next step (its own extra load last)
+                uint4 v = lo[u];
+                if (u + 1 < U && lane == 0)
+                    v = lo[u + 1];
+                const int srcl = (lane + 1) & 31;
+                uint4 nb;
+                nb.x = __shfl_sync(0xffffffffu, v.x, srcl);
+                nb.y = __shfl_sync(0xffffffffu, v.y, srcl);
+                nb.z = __shfl_sync(0xffffffffu, v.z, srcl);
+                nb.w = __shfl_sync(0xffffffffu, v.w, srcl);
+                if (u == U - 1 && lane == 31)
+                    nb = ex;
+                const uint32_t q = (qm[u] >> 4) & 3u;
+                if (q)
+                    o = funnel_words(lo[u], nb, q);
+            }
+            const uint32_t m = qm[u] & 15u;
+            if (m == 0xFu) {
+                st_v4(chunk[u], o);
+            } else if (m) {
+                if (m & 1u) st_u32(chunk[u], o.x);
+                if (m & 2u) st_u32(chunk[u] + 4, o.y);
+                if (m & 4u) st_u32(chunk[u] + 8, o.z);
+                if (m & 8u) st_u32(chunk[u] + 12, o.w);
+            }
+        }
+    }
+}
+
+// Copy tile `ti` (warp-level items) / CTA-level tile `ti` of the plans of a
+// launch, and the pair table of its plan.
+__device__ __forceinline__ int plan_of(const PlanList &L, long long ti, bool copy) {
+    int lo = 0, hi = L.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((copy ? L.p[mid].first_copy : L.p[mid].first_cta) <= ti)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ const Tile *locate_copy(const PlanList &L, long long ti,
+                                                   const PairInfo *&pairs) {
+    const int k = plan_of(L, ti, true);
+    pairs = L.p[k].pairs;
+    return L.p[k].tiles + (ti - L.p[k].first_copy);
+}
+__device__ __forceinline__ const Tile *locate_cta(const PlanList &L, long long ti,
+                                                  const PairInfo *&pairs) {
+    const int k = plan_of(L, ti, false);
+    pairs = L.p[k].pairs;
+    return L.p[k].tiles + L.p[k].n_copy + (ti - L.p[k].first_cta);
+}
+
+// ------------------------------------------------------------ TMA staging
+// The staged kernel keeps several tiles in flight per CTA without holding
+// their data in registers: one lane per column issues a 1-D TMA bulk copy
+// (cp.async.bulk) of the column's 16-byte aligned cover into a ring of
+// shared-memory stages; an mbarrier per stage counts the bytes landed. The
+// CTA then shifts each destination chunk out of shared memory and stores it
+// with 128-bit stores.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Waits for a stage, giving up after `limit_ns` (returns false then).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
+                                                  uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const uint64_t t0 = global_timer_ns();
+    for (uint32_t i = 0; i < (1u << 30); ++i) {
+        if (mbar_try_wait(bar, parity))
+            return true;
+        if (global_timer_ns() - t0 > limit_ns)
+            return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, uint64_t src, uint32_t bytes,
+                                          uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                 "[%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ uint4 lds_v4(uint32_t a) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(a));
+    return v;
+}
+__device__ __forceinline__ uint2 lds_v2(uint32_t a) {
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+
+// Bytes one staged column takes: its 16-byte aligned cover, at most
+// round_up(L, 16) + 16.
+__device__ __forceinline__ int staged_pitch(int L) { return ((L + 15) & ~15) + 16; }
+
+// Plain tiles whose columns are long enough for bulk copies to pay off and
+// whose columns fit one stage.
+__device__ __forceinline__ bool tma_eligible(const Tile &t, int stage_bytes) {
+    if (t.kind & (KIND_TRANS | KIND_SCALED))
+        return false;
+    const int L = t.rows * kind_esz(t.kind);
+    return L >= 256 && (long long)t.cols * staged_pitch(L) <= (long long)stage_bytes;
+}
+
+// Warp 0: start the bulk copies of tile `ti` into `stage` (nothing when the
+// tile is past the end or not eligible).
+__device__ __forceinline__ void issue_stage(const PlanList &list, long long ti, long long n,
+                                            unsigned char *stage, uint32_t bar,
+                                            int stage_bytes) {
+    if (ti >= n)
+        return;
+    const int lane = threadIdx.x & 31;
+    const PairInfo *unused;
+    const Tile t = *locate_copy(list, ti, unused);
+    if (!tma_eligible(t, stage_bytes))
+        return;
+    const int L = t.rows * kind_esz(t.kind);
+    const int pitch = staged_pitch(L);
+    uint32_t total = 0;
+    for (int c = lane; c < t.cols; c += 32) {
+        const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+        total += (uint32_t)(((s + (uint64_t)L + 15u) & ~15ull) - (s & ~15ull));
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        total += __shfl_xor_sync(0xffffffffu, total, off);
+    if (lane == 0) {
+        // order earlier generic-proxy reads of this stage before the async writes
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(bar, total);
+    }
+    __syncwarp();
+    const uint32_t sbase = smem_addr(stage);
+    for (int c = lane; c < t.cols; c += 32) {
+        const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+        const uint64_t a0 = s & ~15ull;
+        const uint32_t len = (uint32_t)(((s + (uint64_t)L + 15u) & ~15ull) - a0);
+        bulk_load(sbase + (uint32_t)(c * pitch), a0, len, bar);
+    }
+}
+
+// All threads: write tile t from its staged columns. Column c's cover starts
+// at stage + c * pitch and holds source byte x at offset x - (s & ~15); the
+// destination chunk at d - d0 + rel reads its words at
+// c * pitch + (s & 15) - d0 + rel. Only words of the destination column are
+// read and written.
+template <int THREADS, int U>
+__device__ __forceinline__ void consume_stage(const Tile &t, const unsigned char *stage) {
+    constexpr int NWARP = THREADS / 32;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int L = t.rows * kind_esz(t.kind);
+    const int pitch = staged_pitch(L);
+    const int cpc = ((t.dst_ld & 15) == 0) ? (((int)(t.dst & 15u) + L + 15) >> 4)
+                                           : ((L + 27) >> 4);
+    int lpc_shift = 0;
+    while (lpc_shift < 5 && (1 << lpc_shift) < cpc)
+        ++lpc_shift;
+    const int lpc = 1 << lpc_shift;
+    const int cpw = 32 >> lpc_shift;
+    const int sub = lane >> lpc_shift;
+    const int kl = lane & (lpc - 1);
+    const int col_step = NWARP * cpw;
+    const int warp_col0 = warp * cpw;
+    const int ncolit =
+        t.cols > warp_col0 ? (t.cols - warp_col0 + col_step - 1) / col_step : 0;
+    const int nkit = (cpc + lpc - 1) >> lpc_shift;
+    const int my_col0 = warp_col0 + sub;
+    const uint32_t sbase = smem_addr(stage);
+
+    int colit = 0, kit = 0;
+    while (colit < ncolit) {
+        uint4 v[U];
+        uint64_t chunk[U];
+        uint32_t wm[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int c = my_col0 + colit * col_step;
+            const bool colok = (colit < ncolit) && (c < t.cols);
+            const uint64_t d = t.dst + (uint64_t)((long long)c * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)c * t.src_ld);
+            const int d0 = (int)(d & 15u);
+            const int off0 = (int)(s & 15u) - d0;
+            const int rel = (kl + (kit << lpc_shift)) << 4;
+            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
+            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
+            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
+            uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
+            m = colok ? m : 0u;
+            const uint32_t sp = sbase + (uint32_t)(c * pitch + off0 + rel);
+            uint4 x = make_uint4(0u, 0u, 0u, 0u);
+            if (m == 0xFu) {
+                if ((off0 & 15) == 0) {
+                    x = lds_v4(sp);
+                } else if ((off0 & 7) == 0) {
+                    const uint2 a = lds_v2(sp), b = lds_v2(sp + 8);
+                    x = make_uint4(a.x, a.y, b.x, b.y);
+                } else {
+                    x = make_uint4(lds_u32(sp), lds_u32(sp + 4), lds_u32(sp + 8),
+                                   lds_u32(sp + 12));
+                }
+            } else if (m) {
+                if (m & 1u) x.x = lds_u32(sp);
+                if (m & 2u) x.y = lds_u32(sp + 4);
+                if (m & 4u) x.z = lds_u32(sp + 8);
+                if (m & 8u) x.w = lds_u32(sp + 12);
+            }
+            v[u] = x;
+            chunk[u] = d - (uint64_t)d0 + (uint64_t)rel;
+            wm[u] = m;
+            if (++kit == nkit) {
+                kit = 0;
+                ++colit;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t m = wm[u];
+            const uint4 o = v[u];
+            if (m == 0xFu) {
+                st_v4(chunk[u], o);
+            } else if (m) {
+                if (m & 1u) st_u32(chunk[u], o.x);
+                if (m & 2u) st_u32(chunk[u] + 4, o.y);
+                if (m & 4u) st_u32(chunk[u] + 8, o.z);
+                if (m & 8u) st_u32(chunk[u] + 12, o.w);
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------- scaled tiles
+struct cplxf {
+    float x, y;
+};
+struct cplxd {
+    double x, y;
+};
+
+template <typename T> __device__ __forceinline__ T ld_elem(uint64_t a);
+template <> __device__ __forceinline__ float ld_elem<float>(uint64_t a) {
+    return *reinterpret_cast<const float *>(a);
+}
+template <> __device__ __forceinline__ double ld_elem<double>(uint64_t a) {
+    return *reinterpret_cast<const double *>(a);
+}
+template <> __device__ __forceinline__ cplxf ld_elem<cplxf>(uint64_t a) {
+    const float *p = reinterpret_cast<const float *>(a);
+    return cplxf{p[0], p[1]};
+}
+template <> __device__ __forceinline__ cplxd ld_elem<cplxd>(uint64_t a) {
+    const double *p = reinterpret_cast<const double *>(a);
+    return cplxd{p[0], p[1]};
+}
+template <typename T> __device__ __forceinline__ void st_elem(uint64_t a, T v);
+template <> __device__ __forceinline__ void st_elem<float>(uint64_t a, float v) {
+    *reinterpret_cast<float *>(a) = v;
+}
+template <> __device__ __forceinline__ void st_elem<double>(uint64_t a, double v) {
+    *reinterpret_cast<double *>(a) = v;
+}
+template <> __device__ __forceinline__ void st_elem<cplxf>(uint64_t a, cplxf v) {
+    float *p = reinterpret_cast<float *>(a);
+    p[0] = v.x;
+    p[1] = v.y;
+}
+template <> __device__ __forceinline__ void st_elem<cplxd>(uint64_t a, cplxd v) {
+    double *p = reinterpret_cast<double *>(a);
+    p[0] = v.x;
+    p[1] = v.y;
+}
+
+__device__ __forceinline__ float conj_elem(float v) { return v; }
+__device__ __forceinline__ double conj_elem(double v) { return v; }
+__device__ __forceinline__ cplxf conj_elem(cplxf v) {
+    v.y = __int_as_float(__float_as_int(v.y) ^ 0x80000000);
+    return v;
+}
+__device__ __forceinline__ cplxd conj_elem(cplxd v) {
+    v.y = __longlong_as_double(__double_as_longlong(v.y) ^ (long long)0x8000000000000000ull);
+    return v;
+}
+
+// Rounded-separately arithmetic (no contraction into FMA).
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+
+// Complex product as GCC computes std::complex<R> * std::complex<R>: the
+// textbook formula with each operation rounded, and when both parts come out
+// NaN the recovery of C99 Annex G (G.5.1, multiplicative operators): boxed
+// infinities, NaN operands set to signed zeros, recomputation scaled by inf.
+template <typename R>
+__device__ __forceinline__ void cmul(R a, R b, R c, R d, R &x, R &y) {
+    const R ac = rmul(a, c), bd = rmul(b, d), ad = rmul(a, d), bc = rmul(b, c);
+    x = rsub(ac, bd);
+    y = radd(ad, bc);
+    if (isnan(x) && isnan(y)) {
+        bool recalc = false;
+        const R one = R(1), zero = R(0);
+        if (isinf(a) || isinf(b)) {
+            a = copysign(isinf(a) ? one : zero, a);
+            b = copysign(isinf(b) ? one : zero, b);
+            if (isnan(c)) c = copysign(zero, c);
+            if (isnan(d)) d = copysign(zero, d);
+            recalc = true;
+        }
+        if (isinf(c) || isinf(d)) {
+            c = copysign(isinf(c) ? one : zero, c);
+            d = copysign(isinf(d) ? one : zero, d);
+            if (isnan(a)) a = copysign(zero, a);
+            if (isnan(b)) b = copysign(zero, b);
+            recalc = true;
+        }
+        if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
+            if (isnan(a)) a = copysign(zero, a);
+            if (isnan(b)) b = copysign(zero, b);
+            if (isnan(c)) c = copysign(zero, c);
+            if (isnan(d)) d = copysign(zero, d);
+            recalc = true;
+        }
+        if (recalc) {
+            const R inf = R(INFINITY);
+            x = rmul(inf, rsub(rmul(a, c), rmul(b, d)));
+            y = rmul(inf, radd(rmul(a, d), rmul(b, c)));
+        }
+    }
+}
+
+// beta*d + alpha*v, as memory_utils.hpp:36 / :111 / :236 evaluate it.
+__device__ __forceinline__ float axpby(float alpha, float v, float beta, float d) {
+    return radd(rmul(beta, d), rmul(alpha, v));
+}
+__device__ __forceinline__ double axpby(double alpha, double v, double beta, double d) {
+    return radd(rmul(beta, d), rmul(alpha, v));
+}
+__device__ __forceinline__ cplxf axpby(cplxf alpha, cplxf v, cplxf beta, cplxf d) {
+    float bx, by, ax, ay;
+    cmul(beta.x, beta.y, d.x, d.y, bx, by);
+    cmul(alpha.x, alpha.y, v.x, v.y, ax, ay);
+    return cplxf{radd(bx, ax), radd(by, ay)};
+}
+__device__ __forceinline__ cplxd axpby(cplxd alpha, cplxd v, cplxd beta, cplxd d) {
+    double bx, by, ax, ay;
+    cmul(beta.x, beta.y, d.x, d.y, bx, by);
+    cmul(alpha.x, alpha.y, v.x, v.y, ax, ay);
+    return cplxd{radd(bx, ax), radd(by, ay)};
+}
+
+template <typename T> __device__ __forceinline__ T scalar_from(const double *v);
+template <> __device__ __forceinline__ float scalar_from<float>(const double *v) {
+    return (float)v[0];
+}
+template <> __device__ __forceinline__ double scalar_from<double>(const double *v) {
+    return v[0];
+}
+template <> __device__ __forceinline__ cplxf scalar_from<cplxf>(const double *v) {
+    return cplxf{(float)v[0], (float)v[1]};
+}
+template <> __device__ __forceinline__ cplxd scalar_from<cplxd>(const double *v) {
+    return cplxd{v[0], v[1]};
+}
+
+template <int THREADS, typename T>
+__device__ __forceinline__ void scaled_tile(const Tile &t, const PairInfo *pairs,
+                                            unsigned char *smem_raw, int td) {
+    constexpr int NWARP = THREADS / 32;
+    constexpr int E = (int)sizeof(T);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const T alpha = scalar_from<T>(pairs[t.pair].alpha);
+    const T beta = scalar_from<T>(pairs[t.pair].beta);
+    const int R = t.rows, C = t.cols;
+    if (!(t.kind & KIND_TRANS)) {
+        for (int c = warp; c < C; c += NWARP) {
+            const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
+            const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+            for (int r = lane; r < R; r += 32) {
+                const T v = ld_elem<T>(sc + (uint64_t)r * E);
+                const T d = ld_elem<T>(dc + (uint64_t)r * E);
+                st_elem<T>(dc + (uint64_t)r * E, axpby(alpha, v, beta, d));
+            }
+        }
+        return;
+    }
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    T *smem = reinterpret_cast<T *>(smem_raw);
+    const int pitch = td + 1;
+    for (int r = warp; r < R; r += NWARP)
+        for (int c = lane; c < C; c += 32)
+            smem[r * pitch + c] =
+                ld_elem<T>(t.src + (uint64_t)((long long)r * t.src_ld + (long long)c * E));
+    __syncthreads();
+    for (int c = warp; c < C; c += NWARP) {
+        const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+        for (int r = lane; r < R; r += 32) {
+            T v = smem[r * pitch + c];
+            if (conj)
+                v = conj_elem(v);
+            const T d = ld_elem<T>(dc + (uint64_t)r * E);
+            st_elem<T>(dc + (uint64_t)r * E, axpby(alpha, v, beta, d));
+        }
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------- pipelined transposed tiles
+// One code path for every element size: each thread holds up to NE elements
+// of a tile as raw 16-byte register slots; the element size and alignment
+// (uniform per tile) pick 4/8/16-byte or split accesses. The CTA-level loop
+// issues the NEXT tile's loads into the slots before it stores the current
+// tile from shared memory, so loads stay in flight across the barriers.
+enum : int { EM_4 = 0, EM_8 = 1, EM_8_SPLIT = 2, EM_16 = 3, EM_16_SPLIT8 = 4, EM_16_SPLIT4 = 5 };
+
+__device__ __forceinline__ int elem_mode(const Tile &t) {
+    const int esz = kind_esz(t.kind);
+    const uint64_t a = t.src | t.dst | (uint64_t)t.src_ld | (uint64_t)t.dst_ld;
+    if (esz == 4)
+        return EM_4;
+    if (esz == 8)
+        return (a & 7u) == 0 ? EM_8 : EM_8_SPLIT;
+    return (a & 15u) == 0 ? EM_16 : ((a & 7u) == 0 ? EM_16_SPLIT8 : EM_16_SPLIT4);
+}
+
+__device__ __forceinline__ uint4 ld_elem_raw(uint64_t a, int mode) {
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    switch (mode) {
+    case EM_4: v.x = ldg_w<uint32_t>(a); break;
+    case EM_8: {
+        const unsigned long long w = ldg_w<unsigned long long>(a);
+        v.x = (uint32_t)w;
+        v.y = (uint32_t)(w >> 32);
+        break;
+    }
+    case EM_8_SPLIT:
+        v.x = ldg_w<uint32_t>(a);
+        v.y = ldg_w<uint32_t>(a + 4);
+        break;
+    case EM_16: v = ldg_v4(a); break;
+    case EM_16_SPLIT8: {
+        const unsigned long long w0 = ldg_w<unsigned long long>(a);
+        const unsigned long long w1 = ldg_w<unsigned long long>(a + 8);
+        v = make_uint4((uint32_t)w0, (uint32_t)(w0 >> 32), (uint32_t)w1, (uint32_t)(w1 >> 32));
+        break;
+    }
+    default:
+        v = make_uint4(ldg_w<uint32_t>(a), ldg_w<uint32_t>(a + 4), ldg_w<uint32_t>(a + 8),
+                       ldg_w<uint32_t>(a + 12));
+        break;
+    }
+    return v;
+}
+
+__device__ __forceinline__ void st_elem_raw(uint64_t a, uint4 v, int mode) {
+    switch (mode) {
+    case EM_4: st_u32(a, v.x); break;
+    case EM_8:
+        st_w<unsigned long long>(a, (unsigned long long)v.x | ((unsigned long long)v.y << 32));
+        break;
+    case EM_8_SPLIT:
+        st_u32(a, v.x);
+        st_u32(a + 4, v.y);
+        break;
+    case EM_16: st_v4(a, v); break;
+    case EM_16_SPLIT8:
+        st_w<unsigned long long>(a, (unsigned long long)v.x | ((unsigned long long)v.y << 32));
+        st_w<unsigned long long>(a + 8, (unsigned long long)v.z | ((unsigned long long)v.w << 32));
+        break;
+    default:
+        st_u32(a, v.x);
+        st_u32(a + 4, v.y);
+        st_u32(a + 8, v.z);
+        st_u32(a + 12, v.w);
+        break;
+    }
+}
+
+__device__ __forceinline__ void sts_elem(unsigned char *p, uint4 v, int esz) {
+    if (esz == 4)
+        *reinterpret_cast<uint32_t *>(p) = v.x;
+    else if (esz == 8)
+        *reinterpret_cast<uint2 *>(p) = make_uint2(v.x, v.y);
+    else
+        *reinterpret_cast<uint4 *>(p) = v;
+}
+
+__device__ __forceinline__ uint4 lds_elem(const unsigned char *p, int esz) {
+    if (esz == 4)
+        return make_uint4(*reinterpret_cast<const uint32_t *>(p), 0u, 0u, 0u);
+    if (esz == 8) {
+        const uint2 w = *reinterpret_cast<const uint2 *>(p);
+        return make_uint4(w.x, w.y, 0u, 0u);
+    }
+    return *reinterpret_cast<const uint4 *>(p);
+}
+
+__device__ __forceinline__ bool is_plain_transpose(const Tile &t) {
+    return (t.kind & KIND_TRANS) && !(t.kind & KIND_SCALED);
+}
+
+// A td x td tile (td a power of two) over a CTA: thread x owns one lane of
+// the tile's contiguous direction and every (THREADS / td)-th line of the
+// other, so its addresses advance by a constant step. The element mode is
+// uniform per tile and a template argument here, so no access branches on it.
+template <int MODE> struct ModeEsz {
+    static constexpr int value = MODE == EM_4 ? 4 : (MODE <= EM_8_SPLIT ? 8 : 16);
+};
+
+// Load view: line r = storage column of the source (= final row), lane c
+// along it (= final column).
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void load_slots_m(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    const int c = threadIdx.x & ((1 << td_shift) - 1);
+    const int r0 = threadIdx.x >> td_shift;
+    const int rstep = THREADS >> td_shift;
+    if (c >= t.cols)
+        return;
+    uint64_t a = t.src + (uint64_t)((long long)r0 * t.src_ld + (long long)c * ESZ);
+    const uint64_t step = (uint64_t)((long long)rstep * t.src_ld);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        if (r0 + i * rstep < t.rows)
+            v[i] = ld_elem_raw(a, MODE);
+        a += step;
+    }
+}
+
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void slots_to_smem_m(const Tile &t, int td_shift,
+                                                const uint4 (&v)[NE], unsigned char *smem) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    const int td = 1 << td_shift;
+    const int c = threadIdx.x & (td - 1);
+    const int r0 = threadIdx.x >> td_shift;
+    const int rstep = THREADS >> td_shift;
+    if (c >= t.cols)
+        return;
+    unsigned char *p = smem + (size_t)(r0 * (td + 1) + c) * ESZ;
+    const int step = rstep * (td + 1) * ESZ;
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        if (r0 + i * rstep < t.rows)
+            sts_elem(p, v[i], ESZ);
+        p += step;
+    }
+}
+
+// Store view: line c = destination storage column (= final column), lane r
+// along it (= final row).
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void smem_to_global_m(const Tile &t, int td_shift,
+                                                 const unsigned char *smem) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    const int td = 1 << td_shift;
+    const int r = threadIdx.x & (td - 1);
+    const int c0 = threadIdx.x >> td_shift;
+    const int cstep = THREADS >> td_shift;
+    if (r >= t.rows)
+        return;
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    const unsigned char *p = smem + (size_t)(r * (td + 1) + c0) * ESZ;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ESZ);
+    const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        if (c0 + i * cstep < t.cols) {
+            uint4 e = lds_elem(p, ESZ);
+            if (conj) { // sign of the imaginary part: top word of the element
+                if (ESZ == 8)
+                    e.y ^= 0x80000000u;
+                else if (ESZ == 16)
+                    e.w ^= 0x80000000u;
+            }
+            st_elem_raw(a, e, MODE);
+        }
+        p += cstep * ESZ;
+        a += step;
+    }
+}
+
+#define G2G_MODE_DISPATCH(FN, ...)                                                  \
+    switch (elem_mode(t)) {                                                         \
+    case EM_4: FN<THREADS, NE, EM_4>(__VA_ARGS__); break;                           \
+    case EM_8: FN<THREADS, NE, EM_8>(__VA_ARGS__); break;                           \
+    case EM_8_SPLIT: FN<THREADS, NE, EM_8_SPLIT>(__VA_ARGS__); break;               \
+    case EM_16: FN<THREADS, NE, EM_16>(__VA_ARGS__); break;                         \
+    case EM_16_SPLIT8: FN<THREADS, NE, EM_16_SPLIT8>(__VA_ARGS__); break;           \
+    default: FN<THREADS, NE, EM_16_SPLIT4>(__VA_ARGS__); break;                     \
+    }
+
+template <int THREADS, int NE>
+__device__ __forceinline__ void load_tile_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    G2G_MODE_DISPATCH(load_slots_m, t, td_shift, v)
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void slots_to_smem(const Tile &t, int td_shift, const uint4 (&v)[NE],
+                                              unsigned char *smem) {
+    G2G_MODE_DISPATCH(slots_to_smem_m, t, td_shift, v, smem)
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void smem_to_global(const Tile &t, int td_shift,
+                                               const unsigned char *smem) {
+    G2G_MODE_DISPATCH(smem_to_global_m, t, td_shift, smem)
+}
+#undef G2G_MODE_DISPATCH
+
+// ------------------------------------------------------------------ kernel
+template <int THREADS>
+__device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *pairs,
+                                                unsigned char *smem, int td) {
+    switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0: scaled_tile<THREADS, float>(t, pairs, smem, td); break;
+    case 1: scaled_tile<THREADS, double>(t, pairs, smem, td); break;
+    case 2: scaled_tile<THREADS, cplxf>(t, pairs, smem, td); break;
+    default: scaled_tile<THREADS, cplxd>(t, pairs, smem, td); break;
+    }
+}
+
+// Tile paths a kernel instance contains; a plan launches the smallest
+// instance that covers its tiles, so the plain copy does not carry the
+// register cost of the scaled complex arithmetic.
+enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
+
+// Register budget: 64 per thread (1024 resident threads per SM), enough for
+// U = 4 chunks per lane in flight on the register path without spilling.
+template <int U, int THREADS> struct MinBlocks {
+    static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
+};
+
+// CTA-level tiles (transposed, scaled) of a launch, static striding, with the
+// next transposed tile's loads issued before the current tile is stored.
+template <int THREADS, int PATHS>
+__device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
+    constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
+    const int td_shift = td >= 32 ? 5 : 4;
+    const long long n = list.total_cta;
+    const long long G = gridDim.x;
+    uint4 v[NE];
+    long long ti = blockIdx.x;
+    Tile cur;
+    const PairInfo *cur_pairs = nullptr;
+    if (ti < n) {
+        cur = *locate_cta(list, ti, cur_pairs);
+        if ((PATHS & PATH_TRANSPOSE) && is_plain_transpose(cur))
+            load_tile_slots<THREADS, NE>(cur, td_shift, v);
+    }
+    while (ti < n) {
+        const long long next = ti + G;
+        // the next descriptor is read now and the one after is pulled into
+        // L2, so neither miss sits between the barriers
+        Tile nxt;
+        const PairInfo *nxt_pairs = nullptr;
+        if (next < n) {
+            nxt = *locate_cta(list, next, nxt_pairs);
+            if (threadIdx.x == 0 && next + G < n) {
+                const PairInfo *unused;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_cta(list, next + G, unused)));
+            }
+        }
+        __syncthreads(); // the previous tile is out of shared memory
+        if ((PATHS & PATH_TRANSPOSE) && is_plain_transpose(cur)) {
+            slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
+            __syncthreads();
+            if (next < n && is_plain_transpose(nxt))
+                load_tile_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
+            smem_to_global<THREADS, NE>(cur, td_shift, smem);
+        } else {
+            if (PATHS & PATH_SCALED)
+                scaled_dispatch<THREADS>(cur, cur_pairs, smem, td);
+            if ((PATHS & PATH_TRANSPOSE) && next < n && is_plain_transpose(nxt))
+                load_tile_slots<THREADS, NE>(nxt, td_shift, v);
+        }
+        if (next < n) {
+            cur = nxt;
+            cur_pairs = nxt_pairs;
+        }
+        ti = next;
+    }
+}
+
+template <int THREADS, int U, int PATHS>
+__global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
+    scatter_kernel(const __grid_constant__ PlanList list, int td) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int NWARP = THREADS / 32;
+    const int warp = threadIdx.x >> 5;
+    // phase 1: plain copies, one warp per tile, so a CTA keeps NWARP tiles in
+    // flight however small the pieces are
+    if (PATHS & PATH_COPY) {
+        const long long GW = (long long)gridDim.x * NWARP;
+        for (long long ti = (long long)blockIdx.x * NWARP + warp; ti < list.total_copy;
+             ti += GW) {
+            const PairInfo *pairs;
+            if ((threadIdx.x & 31) == 0 && ti + GW < list.total_copy) {
+                const PairInfo *unused;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, ti + GW, unused)));
+            }
+            const Tile t = *locate_copy(list, ti, pairs);
+            copy_tile<1, U>(t, 0);
+        }
+    }
+    // phase 2: transposed and scaled tiles, one CTA per tile
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
+        cta_phase<THREADS, PATHS>(list, smem, td);
+}
+
+// ------------------------------------------------------ cp.async copy ring
+// Phase 1 of the ring kernel: the plain copy tiles of a warp form one stream
+// of stages of 32 x U chunks (the chunk sequence of copy_tile, cut into
+// stages; a stage belongs to one tile). The warp keeps RING_D - 1 stages in
+// flight as cp.async 16-byte copies into a per-warp ring in shared memory
+// while it stores the oldest landed stage, so its reads continue across tile
+// boundaries and overlap its own stores. Two stages (one in flight while one
+// is stored) at 16 warps per SM measured best on the layouts tried: deeper
+// rings or more warps put more concurrent column streams on the DRAM and
+// lose row locality. A stage is then stored from shared memory:
+// chunk i of a stage reads its source blocks at ring slots i and i + 1 (slot
+// 32U holds the block after the stage's last chunk, loaded by lane 31).
+// The issuing and the storing side each walk the chunk sequence with their
+// own cursor (column, chunk, column addresses), advanced by additions only.
+// Every wait is cp.async.wait_group, which completes with the copies.
+#ifndef G2G_RING_D
+#define G2G_RING_D 2
+#endif
+constexpr int RING_D = G2G_RING_D; // stages per warp ring (RING_D - 1 in flight)
+
+struct RingRec {        // one stage
+    Tile t;             // the tile, written for a tile's first stage only
+    int valid;          // 0: no stage (the warp's work is done)
+    int pad[3];
+};
+static_assert(sizeof(RingRec) == 64, "RingRec is 64 bytes");
+
+template <int U> __host__ __device__ constexpr int ring_warp_bytes() {
+    return RING_D * (U * 32 + 1) * 16 + RING_D * (int)sizeof(RingRec);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gaddr)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// a ring read, ordered after the wait and warp barrier that make it valid
+__device__ __forceinline__ uint4 lds_ring(uint32_t a) {
+    uint4 v;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(a)
+                 : "memory");
+    return v;
+}
+
+// Per-tile constants of a chunk walk (chunks per column as in copy_tile).
+struct RingTile {
+    uint64_t dst, src;
+    long long dld, sld;     // column strides, bytes
+    long long stepd, steps; // dq columns, bytes
+    int cols, L, cpc, dq, dr, total;
+    bool aligned;
+};
+__device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
+    c.dst = t.dst;
+    c.src = t.src;
+    c.dld = t.dst_ld;
+    c.sld = t.src_ld;
+    c.cols = t.cols;
+    c.L = t.rows * kind_esz(t.kind);
+    c.aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    if (((t.dst_ld | t.src_ld) & 15) == 0) {
+        const int d0 = (int)(t.dst & 15u);
+        const int sh = (int)((t.src - (uint64_t)d0) & 15u);
+        c.cpc = (sh + d0 + c.L + 15) >> 4;
+    } else {
+        c.cpc = c.aligned ? ((c.L + 27) >> 4) : ((c.L + 39) >> 4);
+    }
+    c.dq = 32 / c.cpc;
+    c.dr = 32 - c.dq * c.cpc;
+    c.stepd = (long long)c.dq * c.dld;
+    c.steps = (long long)c.dq * c.sld;
+    c.total = c.cols * c.cpc;
+}
+
+// A lane's position: chunk k of column col, whose addresses are d / s.
+struct RingWalk {
+    uint64_t d, s;
+    int col, k;
+};
+__device__ __forceinline__ void ring_walk_init(RingWalk &w, const RingTile &c, int idx) {
+    w.col = idx / c.cpc;
+    w.k = idx - w.col * c.cpc;
+    w.d = c.dst + (uint64_t)((long long)w.col * c.dld);
+    w.s = c.src + (uint64_t)((long long)w.col * c.sld);
+}
+__device__ __forceinline__ void ring_walk_step(RingWalk &w, const RingTile &c) { // +32 chunks
+    w.col += c.dq;
+    w.k += c.dr;
+    w.d += (uint64_t)c.stepd;
+    w.s += (uint64_t)c.steps;
+    if (w.k >= c.cpc) {
+        w.k -= c.cpc;
+        ++w.col;
+        w.d += (uint64_t)c.dld;
+        w.s += (uint64_t)c.sld;
+    }
+}
+
+// Issues the cp.async copies of one stage into ring slots `slots`.
+template <int U>
+__device__ __forceinline__ void ring_issue(const RingTile &c, RingWalk &w, uint32_t slots,
+                                           int lane) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (w.col < c.cols) {
+            const int d0 = (int)(w.d & 15u);
+            const uint64_t sa = w.s - (uint64_t)d0; // source byte under chunk 0's first byte
+            const int sh = (int)(sa & 15u);
+            const uint64_t base = sa - (uint64_t)sh;
+            const int rel = w.k << 4;
+            const int lo = sh + d0, hi = sh + d0 + c.L;
+            const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+            if (rel < hi && rel + 16 > lo)
+                cp_async16(slot, base + (uint64_t)rel);
+            if (u == U - 1 && lane == 31 && sh != 0 && rel + 16 < hi)
+                cp_async16(slot + 16, base + (uint64_t)(rel + 16));
+        }
+        ring_walk_step(w, c);
+    }
+}
+
+// Stores one landed stage from its ring slots.
+template <int U>
+__device__ __forceinline__ void ring_store(const RingTile &c, RingWalk &w, uint32_t slots,
+                                           int lane) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (w.col < c.cols) {
+            const int d0 = (int)(w.d & 15u);
+            const int rel = w.k << 4;
+            const int end = d0 + c.L;
+            if (rel + 16 > d0 && rel < end) { // the chunk holds destination words
+                const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+                uint4 o = lds_ring(slot);
+                if (!c.aligned) {
+                    const int sh = (int)((w.s - (uint64_t)d0) & 15u);
+                    if (sh)
+                        o = funnel_words(o, lds_ring(slot + 16), (uint32_t)(sh >> 2));
+                }
+                const uint64_t chunk = w.d - (uint64_t)d0 + (uint64_t)rel;
+                if (rel >= d0 && rel + 16 <= end) {
+                    st_v4(chunk, o);
+                } else { // head or tail chunk of the column: whole words
+                    const int wlo = rel >= d0 ? 0 : (d0 - rel) >> 2;
+                    const int whi = rel + 16 <= end ? 4 : (end - rel) >> 2;
+                    if (wlo <= 0 && whi > 0) st_u32(chunk, o.x);
+                    if (wlo <= 1 && whi > 1) st_u32(chunk + 4, o.y);
+                    if (wlo <= 2 && whi > 2) st_u32(chunk + 8, o.z);
+                    if (wlo <= 3 && whi > 3) st_u32(chunk + 12, o.w);
+                }
+            }
+        }
+        ring_walk_step(w, c);
+    }
+}
+
+__device__ __forceinline__ void ring_load_tile(const PlanList &list, long long ti, Tile &t) {
+    if (ti < list.total_copy) {
+        const PairInfo *unused;
+        t = *locate_copy(list, ti, unused);
+    }
+}
+
+// The issuing side: the tile it is in (its descriptor until its first stage
+// is recorded), its walk, and the descriptor of the warp's next tile.
+struct RingIssue {
+    long long ti;
+    Tile cur, nt;
+    RingTile c;
+    RingWalk w;
+    int idx0;
+};
+
+// Fills ring stage `st` from the issuing cursor (or marks it empty) and commits it.
+template <int U>
+__device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q, long long GW,
+                                          uint32_t slots, RingRec &rec, int lane) {
+    if (q.ti < list.total_copy) {
+        if (lane == 0) {
+            if (q.idx0 == 0)
+                rec.t = q.cur;
+            rec.valid = 1;
+        }
+        ring_issue<U>(q.c, q.w, slots, lane);
+        q.idx0 += 32 * U;
+        if (q.idx0 >= q.c.total) { // on to the warp's next tile
+            q.ti += GW;
+            q.idx0 = 0;
+            if (q.ti < list.total_copy) {
+                q.cur = q.nt;
+                ring_tile_init(q.c, q.cur);
+                ring_walk_init(q.w, q.c, lane);
+                ring_load_tile(list, q.ti + GW, q.nt);
+                if (lane == 0 && q.ti + 2 * GW < list.total_copy) {
+                    const PairInfo *unused;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(
+                        locate_copy(list, q.ti + 2 * GW, unused)));
+                }
+            }
+        }
+    } else if (lane == 0) {
+        rec.valid = 0;
+    }
+    cp_async_commit();
+}
+
+template <int U>
+__device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
+                                                int warp, int nwarp) {
+    constexpr int SLOT_BYTES = (U * 32 + 1) * 16;
+    const int lane = threadIdx.x & 31;
+    unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
+    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * SLOT_BYTES);
+    const uint32_t slots0 = smem_addr(wbase);
+    const long long GW = (long long)gridDim.x * nwarp;
+    RingIssue q;
+    q.ti = (long long)blockIdx.x * nwarp + warp;
+    q.idx0 = 0;
+    ring_load_tile(list, q.ti, q.cur);
+    ring_load_tile(list, q.ti + GW, q.nt);
+    if (q.ti < list.total_copy) {
+        ring_tile_init(q.c, q.cur);
+        ring_walk_init(q.w, q.c, lane);
+    }
+#pragma unroll
+    for (int st = 0; st < RING_D - 1; ++st)
+        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(st * SLOT_BYTES), recs[st], lane);
+    // the storing side
+    RingTile c;
+    RingWalk w;
+    int idx0 = 0;
+    c.total = 0;
+    int sp = 0; // stage to store; the stage before it is filled next
+    for (;;) {
+        const int sf = sp == 0 ? RING_D - 1 : sp - 1;
+        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(sf * SLOT_BYTES), recs[sf], lane);
+        cp_async_wait<RING_D - 1>();
+        __syncwarp();
+        if (!recs[sp].valid) // stages are filled in order: nothing after this
+            break;
+        if (idx0 >= c.total) { // the stage starts the next tile
+            ring_tile_init(c, recs[sp].t);
+            ring_walk_init(w, c, lane);
+            idx0 = 0;
+        }
+        ring_store<U>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES), lane);
+        idx0 += 32 * U;
+        __syncwarp();
+        sp = sp + 1 == RING_D ? 0 : sp + 1;
+    }
+    cp_async_wait<0>();
+}
+
+// Registers: the ring kernel runs 16 warps per SM on copy-only plans (one
+// 512-thread CTA, or two of 256), 24 with CTA-level tiles (three of 256).
+template <int THREADS> struct RingMinBlocks {
+    static constexpr int value = (768 / THREADS) > 0 ? (768 / THREADS) : 1;
+};
+
+template <int THREADS, int U, int PATHS>
+__global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS>::value))
+    scatter_ring_kernel(const __grid_constant__ PlanList list, int td) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int NWARP = THREADS / 32;
+    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP);
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
+        __syncthreads(); // the ring's shared memory becomes the CTA tiles'
+        cta_phase<THREADS, PATHS>(list, smem, td);
+    }
+}
+
+// The staged variant: a ring of S shared-memory stages filled by TMA bulk
+// copies (see issue_stage / consume_stage); tiles that are not eligible for
+// staging (short columns, transposed, scaled) run on the direct paths in the
+// same loop. Every wait is bounded: on expiry the CTA records the error in
+// *status, waits (bounded) for its other stages and returns.
+constexpr uint64_t STAGE_WAIT_LIMIT_NS = 2000000000ull; // 2 s
+
+template <int THREADS, int U, int PATHS, int S>
+__global__ void __launch_bounds__(THREADS, 1)
+    scatter_staged_kernel(const __grid_constant__ PlanList list, int td, int stage_bytes) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    unsigned char *stages = smem + 128;
+    unsigned char *direct = stages + (size_t)S * (size_t)stage_bytes;
+    const long long n = list.total_copy;
+    int *status = list.status;
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < S; ++k)
+            mbar_init(smem_addr(&bars[k]), 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const long long G = gridDim.x;
+    if (warp == 0)
+        for (int k = 0; k < S; ++k)
+            issue_stage(list, blockIdx.x + k * G, n, stages + (size_t)k * stage_bytes,
+                        smem_addr(&bars[k]), stage_bytes);
+    uint32_t phase = 0;
+    int st = 0;
+    for (long long ti = blockIdx.x; ti < n; ti += G) {
+        const PairInfo *pairs;
+        const Tile t = *locate_copy(list, ti, pairs);
+        unsigned char *stage = stages + (size_t)st * stage_bytes;
+        const uint32_t bar = smem_addr(&bars[st]);
+        if ((PATHS & PATH_COPY) && tma_eligible(t, stage_bytes)) {
+            const bool ok = mbar_wait_bounded(bar, (phase >> st) & 1u, STAGE_WAIT_LIMIT_NS);
+            if (!__syncthreads_and(ok)) {
+                if (threadIdx.x == 0) {
+                    atomicExch(status, 1);
+                    for (int k = 0; k < S; ++k)
+                        mbar_wait_bounded(smem_addr(&bars[k]), (phase >> k) & 1u,
+                                          STAGE_WAIT_LIMIT_NS / 4);
+                }
+                __syncthreads();
+                return;
+            }
+            phase ^= 1u << st;
+            consume_stage<THREADS, U>(t, stage);
+        } else {
+            copy_tile<THREADS / 32, U>(t, warp);
+        }
+        __syncthreads(); // the stage is free again
+        if (warp == 0)
+            issue_stage(list, ti + (long long)S * G, n, stage, bar, stage_bytes);
+        st = (st + 1 == S) ? 0 : st + 1;
+    }
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
+        cta_phase<THREADS, PATHS>(list, direct, td);
+}
+
+template <typename K>
+cudaError_t prepare(K k, const ScatterConfig &cfg, size_t smem, long long total,
+                    unsigned &grid_out) {
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, cfg.threads, smem);
+    if (e != cudaSuccess)
+        return e;
+    if (occ < 1)
+        return cudaErrorInvalidConfiguration;
+    // a persistent grid must be resident at once (static striding)
+    long long grid = cfg.grid;
+    const long long resident = (long long)cfg.sm_count * occ;
+    if (cfg.sm_count > 0 && grid > resident)
+        grid = resident;
+    if (grid > total)
+        grid = total;
+    grid_out = (unsigned)(grid < 1 ? 1 : grid);
+    return cudaSuccess;
+}
+
+template <int THREADS, int U, int PATHS, int S>
+cudaError_t launch_staged(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
+    auto k = scatter_staged_kernel<THREADS, U, PATHS, S>;
+    const size_t smem = staged_smem_bytes(cfg);
+    unsigned grid = 0;
+    cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim, cfg.stage_bytes);
+    return cudaGetLastError();
+}
+
+template <int THREADS, int U, int PATHS>
+cudaError_t launch_ring(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
+    auto k = scatter_ring_kernel<THREADS, U, PATHS>;
+    const size_t smem = ring_smem_bytes(cfg);
+    unsigned grid = 0;
+    cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim);
+    return cudaGetLastError();
+}
+
+template <int THREADS, int U, int PATHS>
+cudaError_t launch_t(const PlanList &list, const ScatterConfig &cfg, cudaStream_t s) {
+    if constexpr ((PATHS & PATH_COPY) != 0) {
+        if (cfg.ring && cfg.stages < 2)
+            return launch_ring<THREADS, U, PATHS>(list, cfg, s);
+        if (cfg.stages >= 2) {
+            switch (cfg.stages) {
+            case 2: return launch_staged<THREADS, U, PATHS, 2>(list, cfg, s);
+            case 3: return launch_staged<THREADS, U, PATHS, 3>(list, cfg, s);
+            default: return launch_staged<THREADS, U, PATHS, 4>(list, cfg, s);
+            }
+        }
+    }
+    auto k = scatter_kernel<THREADS, U, PATHS>;
+    unsigned grid = 0;
+    cudaError_t e = prepare(k, cfg, cfg.smem_bytes, list.total_copy + list.total_cta, grid);
+    if (e != cudaSuccess)
+        return e;
+    k<<<grid, THREADS, cfg.smem_bytes, s>>>(list, cfg.tile_dim);
+    return cudaGetLastError();
+}
+
+template <int THREADS, int PATHS>
+cudaError_t launch_u(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
+    switch (cfg.unroll) {
+    case 1: return launch_t<THREADS, 1, PATHS>(l, cfg, s);
+    case 2: return launch_t<THREADS, 2, PATHS>(l, cfg, s);
+    default: return launch_t<THREADS, 4, PATHS>(l, cfg, s);
+    }
+}
+
+template <int THREADS>
+cudaError_t launch_p(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
+    if (cfg.paths & PATH_SCALED)
+        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(l, cfg, s);
+    if (cfg.paths == PATH_COPY)
+        return launch_u<THREADS, PATH_COPY>(l, cfg, s);
+    if (cfg.paths == PATH_TRANSPOSE)
+        return launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
+    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
+}
+
+} // namespace
+
+} // namespace g2g
