@@ -980,15 +980,25 @@ __global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
 #endif
 constexpr int RING_D = G2G_RING_D; // stages per warp ring (RING_D - 1 in flight)
 
-struct RingRec {        // one stage
-    Tile t;             // the tile, written for a tile's first stage only
-    int valid;          // 0: no stage (the warp's work is done)
-    int pad[3];
-};
-static_assert(sizeof(RingRec) == 64, "RingRec is 64 bytes");
+// Tile descriptors reach the warp through a queue in shared memory: the
+// descriptor of the warp's tile j + RING_LA is copied (cp.async, in the same
+// commit group as the stage being issued) when the issuing side enters tile
+// j. A stage enters at most one tile and the groups of all but the last
+// RING_D - 1 stages have landed when a stage is issued, so it has landed by
+// the time that tile is entered, however short the tiles in between are. The
+// storing side, at most RING_D - 1 stages behind, reads the same entries.
+constexpr int RING_LA = RING_D;
+constexpr int RING_Q = (2 * RING_D + 1 <= 8) ? 8 : 16; // entries; > RING_LA + RING_D
+constexpr int RING_QE = 64;                            // bytes per entry (a 48-byte Tile)
+static_assert(sizeof(Tile) <= RING_QE, "a Tile fits a queue entry");
 
+// Per-warp shared memory: RING_D stages of 32U + 1 blocks, the descriptor
+// queue, one valid flag per stage (0: no stage, the warp's work is done).
+template <int U> __host__ __device__ constexpr int ring_stage_bytes() {
+    return (U * 32 + 1) * 16;
+}
 template <int U> __host__ __device__ constexpr int ring_warp_bytes() {
-    return RING_D * (U * 32 + 1) * 16 + RING_D * (int)sizeof(RingRec);
+    return RING_D * ring_stage_bytes<U>() + RING_Q * RING_QE + ((RING_D * 4 + 15) / 16) * 16;
 }
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
@@ -1017,6 +1027,7 @@ struct RingTile {
     long long dld, sld;     // column strides, bytes
     long long stepd, steps; // dq columns, bytes
     int cols, L, cpc, dq, dr, total;
+    float rcp; // 1 / cpc, for the quotients of small numbers by cpc
     bool aligned;
 };
 __device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
@@ -1034,7 +1045,10 @@ __device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
     } else {
         c.cpc = c.aligned ? ((c.L + 27) >> 4) : ((c.L + 39) >> 4);
     }
-    c.dq = 32 / c.cpc;
+    // floor(32 / cpc) from a correctly rounded reciprocal: (32 + 1/2) / cpc
+    // lies at least 1/(2 cpc) from an integer, far above the rounding error
+    c.rcp = __frcp_rn((float)c.cpc);
+    c.dq = __float2int_rz(32.5f * c.rcp);
     c.dr = 32 - c.dq * c.cpc;
     c.stepd = (long long)c.dq * c.dld;
     c.steps = (long long)c.dq * c.sld;
@@ -1046,9 +1060,9 @@ struct RingWalk {
     uint64_t d, s;
     int col, k;
 };
-__device__ __forceinline__ void ring_walk_init(RingWalk &w, const RingTile &c, int idx) {
-    w.col = idx / c.cpc;
-    w.k = idx - w.col * c.cpc;
+__device__ __forceinline__ void ring_walk_init(RingWalk &w, const RingTile &c, int lane) {
+    w.col = __float2int_rz(((float)lane + 0.5f) * c.rcp); // lane / cpc, lane < 32
+    w.k = lane - w.col * c.cpc;
     w.d = c.dst + (uint64_t)((long long)w.col * c.dld);
     w.s = c.src + (uint64_t)((long long)w.col * c.sld);
 }
@@ -1123,18 +1137,22 @@ __device__ __forceinline__ void ring_store(const RingTile &c, RingWalk &w, uint3
     }
 }
 
-__device__ __forceinline__ void ring_load_tile(const PlanList &list, long long ti, Tile &t) {
-    if (ti < list.total_copy) {
+// Lanes 0-2 copy the descriptor of copy tile `ti` (if any) into queue entry
+// `entry` (a shared-memory address); tiles are 16-byte aligned in HBM.
+__device__ __forceinline__ void ring_queue_fetch(const PlanList &list, long long ti,
+                                                 uint32_t entry, int lane) {
+    if (lane < 3 && ti < list.total_copy) {
         const PairInfo *unused;
-        t = *locate_copy(list, ti, unused);
+        const uint64_t g = (uint64_t)locate_copy(list, ti, unused);
+        cp_async16(entry + (uint32_t)(lane * 16), g + (uint64_t)(lane * 16));
     }
 }
 
-// The issuing side: the tile it is in (its descriptor until its first stage
-// is recorded), its walk, and the descriptor of the warp's next tile.
+// The issuing side: its tile (index ti, ordinal j among the warp's tiles),
+// the tile's walk constants and this lane's position, the next chunk.
 struct RingIssue {
     long long ti;
-    Tile cur, nt;
+    int j;
     RingTile c;
     RingWalk w;
     int idx0;
@@ -1143,32 +1161,33 @@ struct RingIssue {
 // Fills ring stage `st` from the issuing cursor (or marks it empty) and commits it.
 template <int U>
 __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q, long long GW,
-                                          uint32_t slots, RingRec &rec, int lane) {
+                                          uint32_t slots, const unsigned char *queue,
+                                          uint32_t queue_s, int *valid, int lane) {
     if (q.ti < list.total_copy) {
-        if (lane == 0) {
-            if (q.idx0 == 0)
-                rec.t = q.cur;
-            rec.valid = 1;
-        }
+        if (lane == 0)
+            *valid = 1;
         ring_issue<U>(q.c, q.w, slots, lane);
         q.idx0 += 32 * U;
         if (q.idx0 >= q.c.total) { // on to the warp's next tile
             q.ti += GW;
+            ++q.j;
             q.idx0 = 0;
             if (q.ti < list.total_copy) {
-                q.cur = q.nt;
-                ring_tile_init(q.c, q.cur);
+                ring_tile_init(q.c, *reinterpret_cast<const Tile *>(
+                                        queue + (q.j & (RING_Q - 1)) * RING_QE));
                 ring_walk_init(q.w, q.c, lane);
-                ring_load_tile(list, q.ti + GW, q.nt);
-                if (lane == 0 && q.ti + 2 * GW < list.total_copy) {
+                ring_queue_fetch(list, q.ti + RING_LA * GW,
+                                 queue_s + (uint32_t)(((q.j + RING_LA) & (RING_Q - 1)) * RING_QE),
+                                 lane);
+                if (lane == 0 && q.ti + (RING_LA + 2) * GW < list.total_copy) {
                     const PairInfo *unused;
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(
-                        locate_copy(list, q.ti + 2 * GW, unused)));
+                        locate_copy(list, q.ti + (RING_LA + 2) * GW, unused)));
                 }
             }
         }
     } else if (lane == 0) {
-        rec.valid = 0;
+        *valid = 0;
     }
     cp_async_commit();
 }
@@ -1176,25 +1195,40 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q, lo
 template <int U>
 __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
                                                 int warp, int nwarp) {
-    constexpr int SLOT_BYTES = (U * 32 + 1) * 16;
+    constexpr int SLOT_BYTES = ring_stage_bytes<U>();
     const int lane = threadIdx.x & 31;
     unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
-    RingRec *recs = reinterpret_cast<RingRec *>(wbase + RING_D * SLOT_BYTES);
+    unsigned char *queue = wbase + RING_D * SLOT_BYTES;
+    int *valid = reinterpret_cast<int *>(queue + RING_Q * RING_QE);
     const uint32_t slots0 = smem_addr(wbase);
+    const uint32_t queue_s = smem_addr(queue);
     const long long GW = (long long)gridDim.x * nwarp;
     RingIssue q;
     q.ti = (long long)blockIdx.x * nwarp + warp;
+    q.j = 0;
     q.idx0 = 0;
-    ring_load_tile(list, q.ti, q.cur);
-    ring_load_tile(list, q.ti + GW, q.nt);
+    // descriptors of the first RING_LA + 1 tiles, landed before the first fill
+#pragma unroll
+    for (int k = 0; k <= RING_LA; ++k)
+        ring_queue_fetch(list, q.ti + k * GW, queue_s + (uint32_t)(k * RING_QE), lane);
+    cp_async_commit();
+    if (lane < 2 && q.ti + (RING_LA + 1 + lane) * GW < list.total_copy) {
+        const PairInfo *unused;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(
+            locate_copy(list, q.ti + (RING_LA + 1 + lane) * GW, unused)));
+    }
+    cp_async_wait<0>();
+    __syncwarp();
     if (q.ti < list.total_copy) {
-        ring_tile_init(q.c, q.cur);
+        ring_tile_init(q.c, *reinterpret_cast<const Tile *>(queue));
         ring_walk_init(q.w, q.c, lane);
     }
 #pragma unroll
     for (int st = 0; st < RING_D - 1; ++st)
-        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(st * SLOT_BYTES), recs[st], lane);
-    // the storing side
+        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(st * SLOT_BYTES), queue, queue_s,
+                     valid + st, lane);
+    // the storing side: its tile ordinal, walk constants and position
+    int js = -1;
     RingTile c;
     RingWalk w;
     int idx0 = 0;
@@ -1202,13 +1236,16 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     int sp = 0; // stage to store; the stage before it is filled next
     for (;;) {
         const int sf = sp == 0 ? RING_D - 1 : sp - 1;
-        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(sf * SLOT_BYTES), recs[sf], lane);
+        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(sf * SLOT_BYTES), queue, queue_s,
+                     valid + sf, lane);
         cp_async_wait<RING_D - 1>();
         __syncwarp();
-        if (!recs[sp].valid) // stages are filled in order: nothing after this
+        if (!valid[sp]) // stages are filled in order: nothing after this
             break;
         if (idx0 >= c.total) { // the stage starts the next tile
-            ring_tile_init(c, recs[sp].t);
+            ++js;
+            ring_tile_init(c, *reinterpret_cast<const Tile *>(
+                                  queue + (js & (RING_Q - 1)) * RING_QE));
             ring_walk_init(w, c, lane);
             idx0 = 0;
         }
