@@ -144,6 +144,17 @@ def make_op(trans="N", alpha=1.0, beta=0.0) -> Op:
 # (name, restype, argtypes) of every exported function in the header.
 _VP = C.c_void_p
 _I32P = C.POINTER(C.c_int32)
+class ScalapackDesc(C.Structure):
+    _fields_ = [
+        ("m", C.c_int32), ("n", C.c_int32),
+        ("mb", C.c_int32), ("nb", C.c_int32),
+        ("rsrc", C.c_int32), ("csrc", C.c_int32),
+        ("nprow", C.c_int32), ("npcol", C.c_int32),
+        ("row_major", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
 SIGNATURES = [
     ("g2g_last_error_string", C.c_char_p, []),
     ("g2g_version_string", C.c_char_p, []),
@@ -170,6 +181,16 @@ SIGNATURES = [
     ("g2g_plan_cache_clear", C.c_int, []),
     ("g2g_grid_cover", C.c_int,
      [_I32P, C.c_int32, _I32P, C.c_int32, _I32P, _I32P, _VP]),
+    ("g2g_layout_create_scalapack", C.c_int,
+     [C.POINTER(ScalapackDesc), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+      C.POINTER(_VP), _I32P, C.c_int, C.POINTER(_VP)]),
+    ("g2g_layout_get_desc", C.c_int, [_VP, C.POINTER(LayoutDesc)]),
+    ("g2g_layout_destroy", C.c_int, [_VP]),
+    ("g2g_gemr2d", C.c_int,
+     [C.c_int32, C.c_int32,
+      C.POINTER(_VP), C.c_int32, C.c_int32, C.POINTER(ScalapackDesc), _I32P,
+      C.POINTER(_VP), C.c_int32, C.c_int32, C.POINTER(ScalapackDesc), _I32P,
+      C.c_int, C.POINTER(Op), _VP]),
     ("g2g_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(_VP)]),
     ("g2g_server_submit", C.c_int,
      [_VP, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op),

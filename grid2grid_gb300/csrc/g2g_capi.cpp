@@ -56,13 +56,6 @@ using g2g::fail;
                         cudaGetErrorString(e_), __FILE__, __LINE__);                    \
     } while (0)
 
-#define G2G_TRY(expr)                                                                   \
-    do {                                                                                \
-        g2g_status s_ = (expr);                                                         \
-        if (s_ != G2G_SUCCESS)                                                          \
-            return s_;                                                                  \
-    } while (0)
-
 int dtype_esz(int dt) {
     switch (dt) {
     case G2G_FLOAT32: return 4;

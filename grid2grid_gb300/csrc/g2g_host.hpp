@@ -15,6 +15,14 @@ namespace g2g {
 // returns `st`.
 g2g_status fail(g2g_status st, const char *fmt, ...);
 
+// Returns the status of `expr` from the calling function unless it succeeded.
+#define G2G_TRY(expr)                                                                   \
+    do {                                                                                \
+        g2g_status s_ = (expr);                                                         \
+        if (s_ != G2G_SUCCESS)                                                          \
+            return s_;                                                                  \
+    } while (0)
+
 // m*n*sizeof(T) summed over the plan's pairs (no synchronisation).
 int64_t plan_bytes_moved(const g2g_plan *plan);
 

@@ -258,6 +258,52 @@ g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a,
                           int32_t *start_index, int32_t *end_index,
                           void *stream);
 
+/* ---- ScaLAPACK-descriptor front end ------------------------------------ */
+
+/* A block-cyclic matrix as a ScaLAPACK array descriptor describes it
+ * (M_, N_, MB_, NB_, RSRC_, CSRC_), over an nprow x npcol grid of virtual
+ * ranks. The local leading dimensions (LLD_) are passed per rank. */
+typedef struct g2g_scalapack_desc {
+    int32_t m, n;         /* global rows, columns                              */
+    int32_t mb, nb;       /* rows, columns of a block                          */
+    int32_t rsrc, csrc;   /* process row, column holding the first block       */
+    int32_t nprow, npcol; /* process grid                                      */
+    int32_t row_major;    /* rank = prow*npcol + pcol (1) or pcol*nprow + prow (0) */
+    int32_t reserved;
+} g2g_scalapack_desc;
+
+/* A layout built by the library; it owns the arrays its descriptor points to. */
+typedef struct g2g_layout g2g_layout;
+
+/* The layout of the submatrix A(ia:ia+m-1, ja:ja+n-1) (1-based, as in
+ * ScaLAPACK) of the block-cyclic matrix `desc`, rank r's local array at
+ * DEVICE address rank_data[r] with leading dimension lld[r] elements
+ * (lld == NULL: the rank's local block rows x mb, the reference's default).
+ * Same grid, owners, local offsets and strides as get_scalapack_grid
+ * (scalapack_layout.cpp:178-278) for every rank. m == 0 or n == 0 is an
+ * empty layout. Host only: nothing is read from rank_data. */
+g2g_status g2g_layout_create_scalapack(const g2g_scalapack_desc *desc, int32_t ia,
+                                       int32_t ja, int32_t m, int32_t n,
+                                       void *const *rank_data, const int32_t *lld,
+                                       g2g_dtype dtype, g2g_layout **layout);
+
+/* Points *out at the layout's arrays (valid until g2g_layout_destroy). */
+g2g_status g2g_layout_get_desc(const g2g_layout *layout, g2g_layout_desc *out);
+
+g2g_status g2g_layout_destroy(g2g_layout *layout);
+
+/* p?gemr2d on one GPU: sub(B) = sub(A) between two block-cyclic
+ * distributions, sub(A) = A(ia:ia+m-1, ja:ja+n-1) and sub(B) =
+ * B(ib:ib+m-1, jb:jb+n-1); with `op`, sub(B) = beta*sub(B) + alpha*op(sub(A))
+ * where sub(A) is n x m for 'T' / 'C'. Builds both layouts and runs the
+ * one-shot transform (plans cached, returns after completion). */
+g2g_status g2g_gemr2d(int32_t m, int32_t n,
+                      void *const *a_data, int32_t ia, int32_t ja,
+                      const g2g_scalapack_desc *desc_a, const int32_t *lld_a,
+                      void *const *b_data, int32_t ib, int32_t jb,
+                      const g2g_scalapack_desc *desc_b, const int32_t *lld_b,
+                      g2g_dtype dtype, const g2g_op *op, void *stream);
+
 /* ---- serving: continuous batching ------------------------------------- */
 
 /* A request loop for transforms of device-resident layouts (no counterpart
