@@ -547,40 +547,57 @@ __device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a,
 // NaN the recovery of C99 Annex G (G.5.1, multiplicative operators): boxed
 // infinities, NaN operands set to signed zeros, recomputation scaled by inf.
 template <typename R>
+__device__ __noinline__ void cmul_nan(R a, R b, R c, R d, R ac, R bd, R ad, R bc, R *xo,
+                                      R *yo) {
+    bool recalc = false;
+    const R one = R(1), zero = R(0);
+    if (isinf(a) || isinf(b)) {
+        a = copysign(isinf(a) ? one : zero, a);
+        b = copysign(isinf(b) ? one : zero, b);
+        if (isnan(c)) c = copysign(zero, c);
+        if (isnan(d)) d = copysign(zero, d);
+        recalc = true;
+    }
+    if (isinf(c) || isinf(d)) {
+        c = copysign(isinf(c) ? one : zero, c);
+        d = copysign(isinf(d) ? one : zero, d);
+        if (isnan(a)) a = copysign(zero, a);
+        if (isnan(b)) b = copysign(zero, b);
+        recalc = true;
+    }
+    if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
+        if (isnan(a)) a = copysign(zero, a);
+        if (isnan(b)) b = copysign(zero, b);
+        if (isnan(c)) c = copysign(zero, c);
+        if (isnan(d)) d = copysign(zero, d);
+        recalc = true;
+    }
+    if (recalc) {
+        const R inf = R(INFINITY);
+        *xo = rmul(inf, rsub(rmul(a, c), rmul(b, d)));
+        *yo = rmul(inf, radd(rmul(a, d), rmul(b, c)));
+    }
+}
+
+// NaN tests on the bit patterns (integer pipe: the FP64 pipe of this GPU is
+// narrow and the complex<double> products already load it).
+__device__ __forceinline__ bool nan_bits(float v) {
+    return (__float_as_uint(v) & 0x7fffffffu) > 0x7f800000u;
+}
+__device__ __forceinline__ bool nan_bits(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) >
+           0x7ff0000000000000ull;
+}
+
+// (the recovery, rare, is a separate function so that the common path keeps
+// few registers)
+template <typename R>
 __device__ __forceinline__ void cmul(R a, R b, R c, R d, R &x, R &y) {
     const R ac = rmul(a, c), bd = rmul(b, d), ad = rmul(a, d), bc = rmul(b, c);
     x = rsub(ac, bd);
     y = radd(ad, bc);
-    if (isnan(x) && isnan(y)) {
-        bool recalc = false;
-        const R one = R(1), zero = R(0);
-        if (isinf(a) || isinf(b)) {
-            a = copysign(isinf(a) ? one : zero, a);
-            b = copysign(isinf(b) ? one : zero, b);
-            if (isnan(c)) c = copysign(zero, c);
-            if (isnan(d)) d = copysign(zero, d);
-            recalc = true;
-        }
-        if (isinf(c) || isinf(d)) {
-            c = copysign(isinf(c) ? one : zero, c);
-            d = copysign(isinf(d) ? one : zero, d);
-            if (isnan(a)) a = copysign(zero, a);
-            if (isnan(b)) b = copysign(zero, b);
-            recalc = true;
-        }
-        if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
-            if (isnan(a)) a = copysign(zero, a);
-            if (isnan(b)) b = copysign(zero, b);
-            if (isnan(c)) c = copysign(zero, c);
-            if (isnan(d)) d = copysign(zero, d);
-            recalc = true;
-        }
-        if (recalc) {
-            const R inf = R(INFINITY);
-            x = rmul(inf, rsub(rmul(a, c), rmul(b, d)));
-            y = rmul(inf, radd(rmul(a, d), rmul(b, c)));
-        }
-    }
+    if (nan_bits(x) && nan_bits(y))
+        cmul_nan(a, b, c, d, ac, bd, ad, bc, &x, &y);
 }
 
 // beta*d + alpha*v, as memory_utils.hpp:36 / :111 / :236 evaluate it.
@@ -617,6 +634,170 @@ template <> __device__ __forceinline__ cplxd scalar_from<cplxd>(const double *v)
     return cplxd{v[0], v[1]};
 }
 
+// beta*d + alpha*v on the whole elements of a 16-byte chunk.
+template <typename T> __device__ __forceinline__ uint4 axpby_chunk(T alpha, uint4 v, T beta, uint4 d);
+template <>
+__device__ __forceinline__ uint4 axpby_chunk<float>(float alpha, uint4 v, float beta, uint4 d) {
+    return make_uint4(
+        __float_as_uint(axpby(alpha, __uint_as_float(v.x), beta, __uint_as_float(d.x))),
+        __float_as_uint(axpby(alpha, __uint_as_float(v.y), beta, __uint_as_float(d.y))),
+        __float_as_uint(axpby(alpha, __uint_as_float(v.z), beta, __uint_as_float(d.z))),
+        __float_as_uint(axpby(alpha, __uint_as_float(v.w), beta, __uint_as_float(d.w))));
+}
+__device__ __forceinline__ double dbl(uint32_t lo, uint32_t hi) {
+    return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ void dbl_words(double x, uint32_t &lo, uint32_t &hi) {
+    lo = (uint32_t)__double2loint(x);
+    hi = (uint32_t)__double2hiint(x);
+}
+template <>
+__device__ __forceinline__ uint4 axpby_chunk<double>(double alpha, uint4 v, double beta, uint4 d) {
+    uint4 o;
+    dbl_words(axpby(alpha, dbl(v.x, v.y), beta, dbl(d.x, d.y)), o.x, o.y);
+    dbl_words(axpby(alpha, dbl(v.z, v.w), beta, dbl(d.z, d.w)), o.z, o.w);
+    return o;
+}
+template <>
+__device__ __forceinline__ uint4 axpby_chunk<cplxf>(cplxf alpha, uint4 v, cplxf beta, uint4 d) {
+    const cplxf a = axpby(alpha, cplxf{__uint_as_float(v.x), __uint_as_float(v.y)}, beta,
+                          cplxf{__uint_as_float(d.x), __uint_as_float(d.y)});
+    const cplxf b = axpby(alpha, cplxf{__uint_as_float(v.z), __uint_as_float(v.w)}, beta,
+                          cplxf{__uint_as_float(d.z), __uint_as_float(d.w)});
+    return make_uint4(__float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(b.x),
+                      __float_as_uint(b.y));
+}
+template <>
+__device__ __forceinline__ uint4 axpby_chunk<cplxd>(cplxd alpha, uint4 v, cplxd beta, uint4 d) {
+    const cplxd a = axpby(alpha, cplxd{dbl(v.x, v.y), dbl(v.z, v.w)}, beta,
+                          cplxd{dbl(d.x, d.y), dbl(d.z, d.w)});
+    uint4 o;
+    dbl_words(a.x, o.x, o.y);
+    dbl_words(a.y, o.z, o.w);
+    return o;
+}
+
+// A destination read that stays coherent with this kernel's own writes.
+__device__ __forceinline__ uint4 ld_dst_v4(uint64_t addr) {
+    uint4 v;
+    asm volatile("ld.global.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(addr));
+    return v;
+}
+
+// Scaled non-transposed tile, CTA-wide: copy_tile's chunk walk (NWARP warps
+// in runs of 32 x U chunks) with the destination chunk read as well and
+// beta*d + alpha*s computed on its elements. Needs every element of the
+// destination to sit inside one 16-byte chunk (its address a multiple of
+// min(sizeof(T), 16)), which scaled_tile checks.
+template <int NWARP, int U, typename T>
+__device__ __forceinline__ void scaled_copy_tile(const Tile &t, const int warp, const T alpha,
+                                                 const T beta) {
+    const int lane = threadIdx.x & 31;
+    const int L = t.rows * (int)sizeof(T);
+    if (L <= 0 || t.cols <= 0)
+        return;
+    const bool aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
+    int cpc;
+    if (((t.dst_ld | t.src_ld) & 15) == 0) {
+        const int d0 = (int)(t.dst & 15u);
+        const int sh = (int)((t.src - (uint64_t)d0) & 15u);
+        cpc = (sh + d0 + L + 15) >> 4;
+    } else {
+        cpc = aligned ? ((L + 27) >> 4) : ((L + 39) >> 4);
+    }
+    const int total = t.cols * cpc;
+    int col, k;
+    {
+        const int idx = warp * 32 * U + lane;
+        col = idx / cpc;
+        k = idx - col * cpc;
+    }
+    const int dq = 32 / cpc, dr = 32 - dq * cpc;
+    const int skip = (NWARP - 1) * 32 * U;
+    const int sq = skip / cpc, sr = skip - sq * cpc;
+    for (int base = warp * 32 * U; base < total; base += NWARP * 32 * U) { // warp-uniform
+        uint4 lo[U], dd[U];
+        uint4 ex;
+        uint64_t chunk[U];
+        uint32_t qm[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool colok = col < t.cols;
+            const uint64_t d = t.dst + (uint64_t)((long long)col * t.dst_ld);
+            const uint64_t s = t.src + (uint64_t)((long long)col * t.src_ld);
+            const int d0 = (int)(d & 15u);
+            const uint64_t sa = s - (uint64_t)d0;
+            const int sh = (int)(sa & 15u);
+            const int rel = k << 4;
+            const int lo_lim = sh + d0, hi_lim = sh + d0 + L;
+            const bool need = colok && rel < hi_lim && rel + 16 > lo_lim;
+            lo[u] = need ? ldg_v4(sa - (uint64_t)sh + (uint64_t)rel)
+                         : make_uint4(0u, 0u, 0u, 0u);
+            if (u == U - 1 && !aligned) {
+                const bool nx = colok && lane == 31 && sh != 0 && rel + 16 < hi_lim;
+                ex = nx ? ldg_v4(sa - (uint64_t)sh + (uint64_t)(rel + 16))
+                        : make_uint4(0u, 0u, 0u, 0u);
+            }
+            int wlo = (d0 - rel) >> 2, whi = (d0 + L - rel) >> 2;
+            wlo = wlo < 0 ? 0 : (wlo > 4 ? 4 : wlo);
+            whi = whi < 0 ? 0 : (whi > 4 ? 4 : whi);
+            uint32_t m = ((1u << whi) - 1u) & ~((1u << wlo) - 1u);
+            m = colok ? m : 0u;
+            chunk[u] = d - (uint64_t)d0 + (uint64_t)rel;
+            dd[u] = m ? ld_dst_v4(chunk[u]) : make_uint4(0u, 0u, 0u, 0u);
+            qm[u] = m | ((uint32_t)(sh >> 2) << 4);
+            col += dq;
+            k += dr;
+            if (k >= cpc) {
+                k -= cpc;
+                ++col;
+            }
+        }
+        if (NWARP > 1) {
+            col += sq;
+            k += sr;
+            if (k >= cpc) {
+                k -= cpc;
+                ++col;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            uint4 o = lo[u];
+            if (!aligned) { // tile-uniform
+                uint4 v = lo[u];
+                if (u + 1 < U && lane == 0)
+                    v = lo[u + 1];
+                const int srcl = (lane + 1) & 31;
+                uint4 nb;
+                nb.x = __shfl_sync(0xffffffffu, v.x, srcl);
+                nb.y = __shfl_sync(0xffffffffu, v.y, srcl);
+                nb.z = __shfl_sync(0xffffffffu, v.z, srcl);
+                nb.w = __shfl_sync(0xffffffffu, v.w, srcl);
+                if (u == U - 1 && lane == 31)
+                    nb = ex;
+                const uint32_t q = (qm[u] >> 4) & 3u;
+                if (q)
+                    o = funnel_words(lo[u], nb, q);
+            }
+            const uint32_t m = qm[u] & 15u;
+            if (m) {
+                o = axpby_chunk<T>(alpha, o, beta, dd[u]);
+                if (m == 0xFu) {
+                    st_v4(chunk[u], o);
+                } else {
+                    if (m & 1u) st_u32(chunk[u], o.x);
+                    if (m & 2u) st_u32(chunk[u] + 4, o.y);
+                    if (m & 4u) st_u32(chunk[u] + 8, o.z);
+                    if (m & 8u) st_u32(chunk[u] + 12, o.w);
+                }
+            }
+        }
+    }
+}
+
 template <int THREADS, typename T>
 __device__ __forceinline__ void scaled_tile(const Tile &t, const PairInfo *pairs,
                                             unsigned char *smem_raw, int td) {
@@ -626,37 +807,22 @@ __device__ __forceinline__ void scaled_tile(const Tile &t, const PairInfo *pairs
     const T alpha = scalar_from<T>(pairs[t.pair].alpha);
     const T beta = scalar_from<T>(pairs[t.pair].beta);
     const int R = t.rows, C = t.cols;
-    if (!(t.kind & KIND_TRANS)) {
-        for (int c = warp; c < C; c += NWARP) {
-            const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
-            const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
-            for (int r = lane; r < R; r += 32) {
-                const T v = ld_elem<T>(sc + (uint64_t)r * E);
-                const T d = ld_elem<T>(dc + (uint64_t)r * E);
-                st_elem<T>(dc + (uint64_t)r * E, axpby(alpha, v, beta, d));
-            }
-        }
+    if ((t.dst & (uint64_t)((E < 16 ? E : 16) - 1)) == 0) { // whole elements per chunk
+        scaled_copy_tile<NWARP, 2, T>(t, warp, alpha, beta);
         return;
     }
-    const bool conj = (t.kind & KIND_CONJ) != 0;
-    T *smem = reinterpret_cast<T *>(smem_raw);
-    const int pitch = td + 1;
-    for (int r = warp; r < R; r += NWARP)
-        for (int c = lane; c < C; c += 32)
-            smem[r * pitch + c] =
-                ld_elem<T>(t.src + (uint64_t)((long long)r * t.src_ld + (long long)c * E));
-    __syncthreads();
     for (int c = warp; c < C; c += NWARP) {
+        const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
         const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
         for (int r = lane; r < R; r += 32) {
-            T v = smem[r * pitch + c];
-            if (conj)
-                v = conj_elem(v);
+            const T v = ld_elem<T>(sc + (uint64_t)r * E);
             const T d = ld_elem<T>(dc + (uint64_t)r * E);
             st_elem<T>(dc + (uint64_t)r * E, axpby(alpha, v, beta, d));
         }
     }
-    __syncthreads();
+    (void)smem_raw;
+    (void)td;
+    (void)R;
 }
 
 // ------------------------------------------- pipelined transposed tiles
@@ -860,6 +1026,140 @@ __device__ __forceinline__ void smem_to_global(const Tile &t, int td_shift,
 }
 #undef G2G_MODE_DISPATCH
 
+// ------------------------------------------------- scaled transposed tiles
+// Element words <-> element type.
+template <typename T> __device__ __forceinline__ T from_words(uint4 v);
+template <> __device__ __forceinline__ float from_words<float>(uint4 v) {
+    return __uint_as_float(v.x);
+}
+template <> __device__ __forceinline__ double from_words<double>(uint4 v) {
+    return dbl(v.x, v.y);
+}
+template <> __device__ __forceinline__ cplxf from_words<cplxf>(uint4 v) {
+    return cplxf{__uint_as_float(v.x), __uint_as_float(v.y)};
+}
+template <> __device__ __forceinline__ cplxd from_words<cplxd>(uint4 v) {
+    return cplxd{dbl(v.x, v.y), dbl(v.z, v.w)};
+}
+__device__ __forceinline__ uint4 to_words(float x) {
+    return make_uint4(__float_as_uint(x), 0u, 0u, 0u);
+}
+__device__ __forceinline__ uint4 to_words(double x) {
+    uint4 o = make_uint4(0u, 0u, 0u, 0u);
+    dbl_words(x, o.x, o.y);
+    return o;
+}
+__device__ __forceinline__ uint4 to_words(cplxf x) {
+    return make_uint4(__float_as_uint(x.x), __float_as_uint(x.y), 0u, 0u);
+}
+__device__ __forceinline__ uint4 to_words(cplxd x) {
+    uint4 o;
+    dbl_words(x.x, o.x, o.y);
+    dbl_words(x.y, o.z, o.w);
+    return o;
+}
+
+// A destination element read (coherent with this kernel's writes), by mode.
+__device__ __forceinline__ uint32_t ld_dst_u32(uint64_t a) {
+    uint32_t v;
+    asm volatile("ld.global.u32 %0, [%1];" : "=r"(v) : "l"(a));
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_dst_u64(uint64_t a) {
+    unsigned long long v;
+    asm volatile("ld.global.u64 %0, [%1];" : "=l"(v) : "l"(a));
+    return v;
+}
+template <int MODE> __device__ __forceinline__ uint4 ld_dst_elem(uint64_t a) {
+    if (MODE == EM_4)
+        return make_uint4(ld_dst_u32(a), 0u, 0u, 0u);
+    if (MODE == EM_8) {
+        const unsigned long long w = ld_dst_u64(a);
+        return make_uint4((uint32_t)w, (uint32_t)(w >> 32), 0u, 0u);
+    }
+    if (MODE == EM_8_SPLIT)
+        return make_uint4(ld_dst_u32(a), ld_dst_u32(a + 4), 0u, 0u);
+    if (MODE == EM_16)
+        return ld_dst_v4(a);
+    if (MODE == EM_16_SPLIT8) {
+        const unsigned long long w0 = ld_dst_u64(a), w1 = ld_dst_u64(a + 8);
+        return make_uint4((uint32_t)w0, (uint32_t)(w0 >> 32), (uint32_t)w1,
+                          (uint32_t)(w1 >> 32));
+    }
+    return make_uint4(ld_dst_u32(a), ld_dst_u32(a + 4), ld_dst_u32(a + 8), ld_dst_u32(a + 12));
+}
+
+// smem_to_global_m with beta*d + alpha*e on every element.
+template <int THREADS, int NE, int MODE, typename T>
+__device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int td_shift,
+                                                        const unsigned char *smem, T alpha,
+                                                        T beta) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    static_assert(ESZ == (int)sizeof(T), "element mode matches the element type");
+    const int td = 1 << td_shift;
+    const int r = threadIdx.x & (td - 1);
+    const int c0 = threadIdx.x >> td_shift;
+    const int cstep = THREADS >> td_shift;
+    if (r >= t.rows)
+        return;
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    const unsigned char *p = smem + (size_t)(r * (td + 1) + c0) * ESZ;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ESZ);
+    const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
+    // the destination elements are pulled into L1 together (prefetches hold
+    // no registers), then combined one at a time: the complex arithmetic of
+    // several elements would not fit the register budget
+#pragma unroll
+    for (int i = 0; i < NE; ++i)
+        if (c0 + i * cstep < t.cols)
+            asm volatile("prefetch.global.L1 [%0];" ::"l"(a + (uint64_t)i * step));
+#pragma unroll 1
+    for (int i = 0; i < NE; ++i) {
+        if (c0 + i * cstep < t.cols) {
+            uint4 e = lds_elem(p, ESZ);
+            if (conj) {
+                if (ESZ == 8)
+                    e.y ^= 0x80000000u;
+                else if (ESZ == 16)
+                    e.w ^= 0x80000000u;
+            }
+            const T d = from_words<T>(ld_dst_elem<MODE>(a));
+            st_elem_raw(a, to_words(axpby(alpha, from_words<T>(e), beta, d)), MODE);
+        }
+        p += cstep * ESZ;
+        a += step;
+    }
+}
+
+// Stores a scaled transposed (+ conjugated) tile already staged in shared
+// memory (by the plain transposed path's loads): beta*d + alpha*op(s).
+template <int THREADS, typename T>
+__device__ __forceinline__ void scaled_transpose_store(const Tile &t, const PairInfo *pairs,
+                                                       const unsigned char *smem, int td) {
+    constexpr int NE = 1024 / THREADS;
+    const int td_shift = td >= 32 ? 5 : 4;
+    const T alpha = scalar_from<T>(pairs[t.pair].alpha);
+    const T beta = scalar_from<T>(pairs[t.pair].beta);
+    const int mode = elem_mode(t);
+    if constexpr (sizeof(T) == 4) {
+        smem_to_global_scaled_m<THREADS, NE, EM_4, T>(t, td_shift, smem, alpha, beta);
+    } else if constexpr (sizeof(T) == 8) {
+        if (mode == EM_8)
+            smem_to_global_scaled_m<THREADS, NE, EM_8, T>(t, td_shift, smem, alpha, beta);
+        else
+            smem_to_global_scaled_m<THREADS, NE, EM_8_SPLIT, T>(t, td_shift, smem, alpha, beta);
+    } else {
+        if (mode == EM_16)
+            smem_to_global_scaled_m<THREADS, NE, EM_16, T>(t, td_shift, smem, alpha, beta);
+        else if (mode == EM_16_SPLIT8)
+            smem_to_global_scaled_m<THREADS, NE, EM_16_SPLIT8, T>(t, td_shift, smem, alpha,
+                                                                   beta);
+        else
+            smem_to_global_scaled_m<THREADS, NE, EM_16_SPLIT4, T>(t, td_shift, smem, alpha,
+                                                                   beta);
+    }
+}
+
 // ------------------------------------------------------------------ kernel
 template <int THREADS>
 __device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *pairs,
@@ -869,6 +1169,16 @@ __device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *p
     case 1: scaled_tile<THREADS, double>(t, pairs, smem, td); break;
     case 2: scaled_tile<THREADS, cplxf>(t, pairs, smem, td); break;
     default: scaled_tile<THREADS, cplxd>(t, pairs, smem, td); break;
+    }
+}
+template <int THREADS>
+__device__ __forceinline__ void scaled_transpose_dispatch(const Tile &t, const PairInfo *pairs,
+                                                          const unsigned char *smem, int td) {
+    switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0: scaled_transpose_store<THREADS, float>(t, pairs, smem, td); break;
+    case 1: scaled_transpose_store<THREADS, double>(t, pairs, smem, td); break;
+    case 2: scaled_transpose_store<THREADS, cplxf>(t, pairs, smem, td); break;
+    default: scaled_transpose_store<THREADS, cplxd>(t, pairs, smem, td); break;
     }
 }
 
@@ -882,12 +1192,23 @@ enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
 template <int U, int THREADS> struct MinBlocks {
     static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
 };
+// Kernels with scaled tiles: 128 registers (512 resident threads per SM),
+// room for the complex arithmetic of the scaled paths without spilling.
+template <int PATHS, int U, int THREADS> struct MinBlocksP {
+    static constexpr int value = (PATHS & PATH_SCALED)
+                                     ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
+                                     : MinBlocks<U, THREADS>::value;
+};
 
 // CTA-level tiles (transposed, scaled) of a launch, static striding, with the
 // next transposed tile's loads issued before the current tile is stored.
 template <int THREADS, int PATHS>
 __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
     constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
+    // Kernels with scaled tiles move plain transposed tiles one at a time:
+    // the next tile's loads held across the scaled arithmetic would cost
+    // more registers than the overlap gains.
+    constexpr bool PIPE = (PATHS & PATH_TRANSPOSE) && !(PATHS & PATH_SCALED);
     const int td_shift = td >= 32 ? 5 : 4;
     const long long n = list.total_cta;
     const long long G = gridDim.x;
@@ -897,7 +1218,7 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     const PairInfo *cur_pairs = nullptr;
     if (ti < n) {
         cur = *locate_cta(list, ti, cur_pairs);
-        if ((PATHS & PATH_TRANSPOSE) && is_plain_transpose(cur))
+        if (PIPE && is_plain_transpose(cur))
             load_tile_slots<THREADS, NE>(cur, td_shift, v);
     }
     while (ti < n) {
@@ -913,17 +1234,25 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_cta(list, next + G, unused)));
             }
         }
-        __syncthreads(); // the previous tile is out of shared memory
-        if ((PATHS & PATH_TRANSPOSE) && is_plain_transpose(cur)) {
+        const bool staged = (PATHS & PATH_SCALED) ? (cur.kind & KIND_TRANS) != 0
+                                                  : is_plain_transpose(cur);
+        if ((PATHS & (PATH_TRANSPOSE | PATH_SCALED)) && staged) {
+            __syncthreads(); // earlier tiles are out of shared memory
+            // transposed tiles, plain or scaled, staged through shared memory
+            if (!PIPE)
+                load_tile_slots<THREADS, NE>(cur, td_shift, v);
             slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
             __syncthreads();
-            if (next < n && is_plain_transpose(nxt))
+            if (PIPE && next < n && is_plain_transpose(nxt))
                 load_tile_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
-            smem_to_global<THREADS, NE>(cur, td_shift, smem);
+            if ((PATHS & PATH_SCALED) && (cur.kind & KIND_SCALED))
+                scaled_transpose_dispatch<THREADS>(cur, cur_pairs, smem, td);
+            else
+                smem_to_global<THREADS, NE>(cur, td_shift, smem);
         } else {
             if (PATHS & PATH_SCALED)
                 scaled_dispatch<THREADS>(cur, cur_pairs, smem, td);
-            if ((PATHS & PATH_TRANSPOSE) && next < n && is_plain_transpose(nxt))
+            if (PIPE && next < n && is_plain_transpose(nxt))
                 load_tile_slots<THREADS, NE>(nxt, td_shift, v);
         }
         if (next < n) {
@@ -935,7 +1264,7 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
 }
 
 template <int THREADS, int U, int PATHS>
-__global__ void __launch_bounds__(THREADS, (MinBlocks<U, THREADS>::value))
+__global__ void __launch_bounds__(THREADS, (MinBlocksP<PATHS, U, THREADS>::value))
     scatter_kernel(const __grid_constant__ PlanList list, int td) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;
@@ -1259,12 +1588,14 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
 
 // Registers: the ring kernel runs 16 warps per SM on copy-only plans (one
 // 512-thread CTA, or two of 256), 24 with CTA-level tiles (three of 256).
-template <int THREADS> struct RingMinBlocks {
-    static constexpr int value = (768 / THREADS) > 0 ? (768 / THREADS) : 1;
+template <int THREADS, int PATHS> struct RingMinBlocks {
+    static constexpr int value = (PATHS & PATH_SCALED)
+                                     ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
+                                     : ((768 / THREADS) > 0 ? (768 / THREADS) : 1);
 };
 
 template <int THREADS, int U, int PATHS>
-__global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS>::value))
+__global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS, PATHS>::value))
     scatter_ring_kernel(const __grid_constant__ PlanList list, int td) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;
