@@ -369,6 +369,11 @@ def run_ours(args):
         e2e = run_e2e(lib, w, dev_i, dev_f, args.e2e_steps, stream, ws)
     capi.check(lib.g2g_plan_destroy(plan))
 
+    # the scaled form on the same layouts: final = 0.5*final + 2*initial
+    scaled = None
+    if args.batch and rank == 0 and w.ops is None:
+        scaled = run_scaled(lib, w, dI, dF, dts, stream, peak, args.steps // 4 or 1)
+
     batched = serving = None
     if args.batch and rank == 0:
         batched, pool = run_batched(lib, dev, stream, 20, peak)
@@ -396,7 +401,7 @@ def run_ours(args):
             "data": "synthetic (seeded random bit patterns, device-resident)",
             "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
-            "batched_stream": batched, "serving": serving,
+            "batched_stream": batched, "serving": serving, "scaled": scaled,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
                      "tuning": {k: getattr(info.tuning, k) for k in
@@ -444,6 +449,25 @@ def _time_steps(stream, fn, steps, warmup):
         b.record(stream)
     stream.synchronize()
     return a.elapsed_time(b) / steps
+
+
+def run_scaled(lib, w, dI, dF, dts, stream, peak, steps):
+    """final = beta*final + alpha*initial with (alpha, beta) = (2, 0.5) on the
+    headline layouts (traffic 3x the bytes moved: the destination is read)."""
+    from grid2grid_gb300 import capi
+    n = len(w.inits)
+    ops = (capi.Op * n)(*[capi.make_op("N", 2.0, 0.5) for _ in range(n)])
+    sp = C.c_void_p(stream.cuda_stream)
+    plan = C.c_void_p()
+    capi.check(lib.g2g_plan_create_batch(n, dI, dF, dts, ops, sp, C.byref(plan)))
+    info = capi.PlanInfo()
+    capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
+    ms = _time_steps(stream, lambda: capi.check(lib.g2g_plan_execute(plan, sp)), steps, 3)
+    capi.check(lib.g2g_plan_destroy(plan))
+    return {"op": "N, alpha=2, beta=0.5", "ms_per_step": round(ms, 4),
+            "value": round(info.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
+            "traffic_bytes": info.bytes_min_traffic,
+            "roofline_frac": round(info.bytes_min_traffic / (ms * 1e-3) / 1e9 / peak, 4)}
 
 
 def run_batched(lib, dev, stream, steps, peak):

@@ -258,6 +258,28 @@ g2g_status g2g_grid_cover(const int32_t *splits_a, int32_t n_a,
                           int32_t *start_index, int32_t *end_index,
                           void *stream);
 
+/* ---- rank reordering --------------------------------------------------- */
+
+/* communication_volume (transform.cpp:9-39): the elements each pair of
+ * virtual ranks exchanges in a transform from `initial` to `final_`, owners
+ * taken through the layouts' reorderings (grid2D.cpp:116-122). `volume` is
+ * an n_ranks x n_ranks row-major array: entry [r*n_ranks + s], r <= s, holds
+ * the elements moved between r and s (r == s: elements that stay on r);
+ * entries below the diagonal are 0. Only splits and owners are read (no
+ * blocks, no device work). n_ranks must cover every owner. */
+g2g_status g2g_communication_volume(const g2g_layout_desc *initial,
+                                    const g2g_layout_desc *final_, int32_t n_ranks,
+                                    int64_t *volume);
+
+/* optimal_reordering (ranks_reordering.cpp:4-61): a greedy matching on the
+ * volumes that relabels ranks so that more data stays local. Edge r-s weighs
+ * vol(r,s) - vol(r,r) - vol(s,s) (a rank kept where it is weighs 1); edges
+ * are taken by decreasing weight, each rank in at most one, and a taken edge
+ * r-s swaps r and s. Ties are taken in (r, s) order. permutation[r] is r's
+ * new label; *reordered = 1 if it is not the identity. */
+g2g_status g2g_optimal_reordering(const int64_t *volume, int32_t n_ranks,
+                                  int32_t *permutation, int32_t *reordered);
+
 /* ---- ScaLAPACK-descriptor front end ------------------------------------ */
 
 /* A block-cyclic matrix as a ScaLAPACK array descriptor describes it

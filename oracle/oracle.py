@@ -93,6 +93,10 @@ def ref():
         lib.g2g_ref_scalapack_grid_simple.restype = C.c_int
         lib.g2g_ref_scalapack_grid_simple.argtypes = [C.c_int] * 9 + [
             I, I, I, I, I, I, I, I, C.POINTER(C.c_longlong), I, C.POINTER(C.c_longlong)]
+        lib.g2g_ref_comm_volume.restype = C.c_int
+        lib.g2g_ref_comm_volume.argtypes = [
+            C.POINTER(capi.LayoutDesc), C.POINTER(capi.LayoutDesc), C.c_int,
+            C.POINTER(C.c_longlong), I, I, C.c_int]
         lib.g2g_ref_initialize_locally.restype = C.c_longlong
         lib.g2g_ref_initialize_locally.argtypes = [C.POINTER(C.c_double)] + [C.c_int] * 9
         _ref = lib
@@ -164,3 +168,23 @@ def decomp_cover(a, b, which="port"):
     k = fn(a.ctypes.data_as(IP), len(a), b.ctypes.data_as(IP), len(b),
            s.ctypes.data_as(IP), e.ctypes.data_as(IP))
     return s[:k].copy(), e[:k].copy()
+
+
+def ref_comm_volume(Li, Lf, P, presize=True):
+    """The reference's communication_volume and optimal_reordering on two
+    layouts' grids: (P x P volume matrix, permutation, reordered). presize
+    inserts every rank's self entry into the volume map first (see
+    ref_driver.cpp: the reference's own loop inserts them while iterating)."""
+    lib = ref()
+    di, k1 = Li.desc(0)
+    df, k2 = Lf.desc(0)
+    vol = np.zeros(P * P, dtype=np.int64)
+    perm = np.zeros(P, dtype=np.int32)
+    re = C.c_int(0)
+    rc = lib.g2g_ref_comm_volume(C.byref(di), C.byref(df), P,
+                                 vol.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                 perm.ctypes.data_as(C.POINTER(C.c_int)), C.byref(re),
+                                 1 if presize else 0)
+    if rc != 0:
+        raise RuntimeError(lib.g2g_ref_last_error().decode())
+    return vol.reshape(P, P), perm, bool(re.value)

@@ -13,6 +13,7 @@
 #include <grid2grid/grid_cover.hpp>
 #include <grid2grid/scalapack_layout.hpp>
 #include <grid2grid/transform.hpp>
+#include <grid2grid/ranks_reordering.hpp>
 #include <grid2grid/transformer.hpp>
 
 #include "../include/grid2grid_gb300.h"
@@ -306,6 +307,42 @@ long long g2g_ref_initialize_locally(double *buffer, int m, int n, int mb, int n
         scalapack::initialize_locally(buffer, f, rank, dl);
     }
     return (long long)sz;
+}
+
+// communication_volume and optimal_reordering of the reference on the grids
+// of two layouts. volume: P x P row-major, entry [r*P + s] for the edge
+// {r, s} (r <= s); perm: P entries. Returns 0, or -1 with the error set.
+// presize: 1 = every self entry {r, r} inserted (volume 0) before
+// optimal_reordering runs. The reference's loop inserts them itself while it
+// iterates the same unordered_map (ranks_reordering.cpp:28-29), so without
+// them its result depends on when the map rehashes.
+int g2g_ref_comm_volume(const g2g_layout_desc *init, const g2g_layout_desc *fin, int P,
+                        long long *volume, int *perm, int *reordered, int presize) {
+    g_error.clear();
+    try {
+        grid2grid::grid_layout<double> li = build_layout<double>(*init, -1);
+        grid2grid::grid_layout<double> lf = build_layout<double>(*fin, -1);
+        grid2grid::comm_volume cv = grid2grid::communication_volume(li.grid, lf.grid);
+        if (presize)
+            for (int r = 0; r < P; ++r)
+                cv.volume[grid2grid::edge_t{r, r}] += 0;
+        for (int k = 0; k < P * P; ++k)
+            volume[k] = 0;
+        for (const auto &e : cv.volume) {
+            if (e.first.src < 0 || e.first.dest >= P || e.first.src >= P)
+                throw std::runtime_error("rank outside P");
+            volume[(size_t)e.first.src * P + e.first.dest] = e.second;
+        }
+        bool re = false;
+        std::vector<int> p = grid2grid::optimal_reordering(cv, P, re);
+        for (int r = 0; r < P; ++r)
+            perm[r] = p[r];
+        *reordered = re ? 1 : 0;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return -1;
+    }
+    return 0;
 }
 
 } // extern "C"

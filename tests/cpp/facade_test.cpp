@@ -5,13 +5,17 @@
 // result with validate -- here with P virtual ranks as threads, device
 // buffers, and a gpu_communicator in place of MPI_COMM_WORLD. Also covers
 // the 'T' / 'C' overload with alpha/beta, the vector overload through
-// transformer<T>, transform_all_ranks, and error behaviour.
+// transformer<T>, transform_all_ranks, error behaviour, and
+// communication_volume / optimal_reordering (what a caller runs before
+// relabeling its ranks).
+#include <grid2grid/ranks_reordering.hpp>
 #include <grid2grid/scalapack_layout.hpp>
 #include <grid2grid/transform.hpp>
 #include <grid2grid/transformer.hpp>
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <complex>
 #include <cstdio>
@@ -179,6 +183,40 @@ static bool all_ranks_and_errors() {
     return ok;
 }
 
+// communication_volume covers every element once; the relabeling from
+// optimal_reordering keeps at least as much local as the identity.
+static bool reordering_volume(int m, int n) {
+    const int P = 6;
+    scalapack::data_layout l1({m, n}, {40, 30}, {2, 3}, scalapack::column_major);
+    scalapack::data_layout l2({m, n}, {25, 70}, {3, 2}, scalapack::row_major);
+    std::vector<double> dummy(1);
+    grid_layout<double> a = get_scalapack_grid(l1, dummy.data(), 0);
+    grid_layout<double> b = get_scalapack_grid(l2, dummy.data(), 0);
+    comm_volume v = communication_volume(a.grid, b.grid);
+    long long all = 0, local = 0;
+    for (const auto &kv : v.volume) {
+        all += kv.second;
+        if (kv.first.src == kv.first.dest)
+            local += kv.second;
+    }
+    bool re = false;
+    std::vector<int> perm = optimal_reordering(v, P, re);
+    b.reorder_ranks(perm);
+    comm_volume v2 = communication_volume(a.grid, b.grid);
+    long long local2 = 0;
+    for (const auto &kv : v2.volume)
+        if (kv.first.src == kv.first.dest)
+            local2 += kv.second;
+    std::vector<int> sorted = perm;
+    std::sort(sorted.begin(), sorted.end());
+    bool ok = all == (long long)m * n && local2 >= local;
+    for (int r = 0; r < P; ++r)
+        ok = ok && sorted[r] == r;
+    std::printf("reordering_volume %dx%d: %s (local %lld -> %lld of %lld, reordered %d)\n", m, n,
+                ok ? "ok" : "FAILED", local, local2, all, (int)re);
+    return ok;
+}
+
 int main() {
     bool ok = true;
     // the reference's four ctest cases (examples/CMakeLists.txt:20-30)
@@ -190,6 +228,7 @@ int main() {
     ok &= scalapack2scalapack(1000, 777, 32, 17, 100, 61, 3, 4);
     ok &= conjugate_scaled(150, 83);
     ok &= all_ranks_and_errors();
+    ok &= reordering_volume(600, 500);
     std::printf(ok ? "ALL OK\n" : "SOME FAILED\n");
     return ok ? 0 : 1;
 }
