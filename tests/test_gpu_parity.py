@@ -332,3 +332,23 @@ def test_one_shot_plan_cache_reuse():
         want = T.port_run([Li], [Lf], [src], [af], [("T", 1.0, 0.0)])[0]
         T.assert_arenas_equal(df.cpu().numpy(), want, Lf, what=f"cached one-shot {trial}")
     capi.check(lib.g2g_plan_cache_clear())
+
+
+@pytest.mark.parametrize("tuning", [
+    dict(threads=512, unroll=4, ring=1), dict(threads=256, unroll=1, ring=1),
+    dict(threads=512, unroll=2, ring=1, tile_bytes=512), dict(threads=256, unroll=4, ring=-1)])
+def test_tiny_pieces_and_short_tiles(tuning):
+    """Grids with extents of 1-3 elements: hundreds of thousands of pieces a
+    few chunks long, so a warp's stages cross many tile boundaries and its
+    descriptor queue turns over constantly; mixed element sizes in one batch;
+    a tiny pair whose tiles are fewer than the warps of the grid."""
+    rng = np.random.default_rng(4242)
+    inits, finals, ias, fas = [], [], [], []
+    for dt, m, n, hi in [(capi.FLOAT32, 300, 260, 3), (capi.COMPLEX128, 97, 120, 2),
+                         (capi.FLOAT64, 200, 333, 5), (capi.COMPLEX64, 3, 2, 1)]:
+        Li, Lf, ai, af = _random_case(rng, dt, "N", m, n, 7, ext_lo=1, ext_hi=hi)
+        inits.append(Li); finals.append(Lf); ias.append(ai); fas.append(af)
+    want = T.port_run(inits, finals, ias, fas)
+    got = T.gpu_run(inits, finals, ias, fas, how="plan", tuning=tuning, executes=2)
+    for k in range(len(inits)):
+        T.assert_arenas_equal(got[k], want[k], finals[k], what=f"{tuning} pair {k}")
