@@ -347,6 +347,7 @@ struct g2g_plan {
     bool any_trans = false;
     int max_trans_esz = 0;
     int paths = 0; // tile paths the work list needs (1 copy, 2 transpose, 4 scaled)
+    bool host_memory = false; // some block lives in pinned host memory
     g2g_tuning tuning;
     // device
     void *dmem = nullptr;
@@ -529,22 +530,43 @@ void assemble(g2g_plan &pl) {
 
 // Makes the device that holds the plan's blocks current for this library's
 // runtime (callers such as torch keep their own current-device state).
+// Picks the device of the plan's device-memory blocks and notes blocks in
+// pinned host memory (reachable from the GPU at the same address: the kernel
+// then reads or writes them over the host link). Pageable memory is refused.
+// Attributes are looked up once per 2 MB of address space.
 g2g_status bind_device(g2g_plan &pl) {
+    std::unordered_map<uintptr_t, int> seen; // 2 MB region -> cudaMemoryType
+    int device = -1;
     for (const PairHost &p : pl.host)
         for (const HLayout *L : {&p.a, &p.b})
             for (const HBlock &b : L->blocks) {
                 if (!b.data)
                     continue;
-                cudaPointerAttributes attr;
-                G2G_CUDA(cudaPointerGetAttributes(&attr, (const void *)(uintptr_t)b.data));
-                if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
-                    return fail(G2G_ERROR_INVALID_ARGUMENT,
-                                "block data at %p is not device memory (use the host-layout "
-                                "transform for host buffers)",
-                                (void *)(uintptr_t)b.data);
-                G2G_CUDA(cudaSetDevice(attr.device));
-                return G2G_SUCCESS;
+                const uintptr_t region = (uintptr_t)b.data >> 21;
+                auto it = seen.find(region);
+                int type;
+                if (it != seen.end()) {
+                    type = it->second;
+                } else {
+                    cudaPointerAttributes attr;
+                    G2G_CUDA(cudaPointerGetAttributes(&attr, (const void *)(uintptr_t)b.data));
+                    type = (int)attr.type;
+                    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+                        if (device < 0)
+                            device = attr.device;
+                    } else if (attr.type != cudaMemoryTypeHost) {
+                        return fail(G2G_ERROR_INVALID_ARGUMENT,
+                                    "block data at %p is neither device memory nor pinned host "
+                                    "memory (pin it with cudaHostRegister / cudaHostAlloc)",
+                                    (void *)(uintptr_t)b.data);
+                    }
+                    seen.emplace(region, type);
+                }
+                if (type == (int)cudaMemoryTypeHost)
+                    pl.host_memory = true;
             }
+    if (device >= 0)
+        G2G_CUDA(cudaSetDevice(device));
     return G2G_SUCCESS;
 }
 
@@ -674,9 +696,10 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
                                     : 0;
     c.trans_bytes = c.smem_bytes;
     c.paths = pl.paths ? pl.paths : 1;
-    c.ring = pl.tuning.ring == 1 ? 1 : 0;
+    // blocks in host memory take the register path: plain loads and stores
+    c.ring = (pl.tuning.ring == 1 && !pl.host_memory) ? 1 : 0;
     c.stages = 0;
-    if ((c.paths & 1) && pl.tuning.stages >= 2) {
+    if ((c.paths & 1) && pl.tuning.stages >= 2 && !pl.host_memory) {
         c.stage_bytes = g2g::stage_bytes_for(pl.tuning.tile_bytes);
         int st = pl.tuning.stages;
         while (st >= 2 && 128 + (size_t)st * c.stage_bytes + c.trans_bytes > kMaxSmemPerCta)
@@ -713,6 +736,10 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
     long long tiles = 0;
     for (int k = 0; k < n; ++k) {
         const g2g::ScatterConfig ck = scatter_config(*plans[k]);
+        if (plans[k]->host_memory) {
+            c.ring = 0;
+            c.stages = 0;
+        }
         c.paths |= ck.paths;
         c.trans_bytes = std::max(c.trans_bytes, ck.trans_bytes);
         c.smem_bytes = std::max(c.smem_bytes, ck.smem_bytes);
@@ -773,7 +800,11 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
     // the previous one is stored): more concurrent column streams lose DRAM
     // locality. With CTA-level tiles as well, 256-thread CTAs keep more of
     // those in flight.
-    if (pl->n_copy > 0) {
+    if (pl->host_memory) {
+        // the register path at full occupancy: more in flight over the host link
+        pl->tuning.threads = 256;
+        pl->tuning.ctas_per_sm = 8;
+    } else if (pl->n_copy > 0) {
         const bool cta_tiles = pl->n_tiles > pl->n_copy;
         pl->tuning.threads = cta_tiles ? 256 : 512;
         pl->tuning.ctas_per_sm = cta_tiles ? 3 : 2;

@@ -16,7 +16,10 @@
  * Conventions
  *  - Every function returns a g2g_status; on failure a human-readable message
  *    is available from g2g_last_error_string() (thread-local).
- *  - Pointers in g2g_block_desc.data are DEVICE addresses owned by the caller.
+ *  - Pointers in g2g_block_desc.data are DEVICE addresses owned by the caller,
+ *    or addresses in PINNED host memory (cudaHostAlloc / cudaHostRegister),
+ *    which the gather-scatter then reads or writes in place over the host
+ *    link. Pageable host memory is refused (G2G_ERROR_INVALID_ARGUMENT).
  *    The library never frees them and never touches a destination block's
  *    padding (rows < stride).
  *  - A `stream` argument is a cudaStream_t passed as void* (NULL = legacy
@@ -83,7 +86,7 @@ typedef struct g2g_block_desc {
     int32_t conjugate_on_copy; /* block<T>::conjugate_on_copy (0/1)         */
     int32_t reserved;
     int64_t stride;            /* leading dimension in elements             */
-    void *data;                /* device address of element (0,0)           */
+    void *data;                /* address of element (0,0): device or pinned host */
 } g2g_block_desc;
 
 /* A grid_layout over P virtual ranks (grid_layout.hpp:7-63): the grid, the
