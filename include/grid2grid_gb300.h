@@ -34,6 +34,9 @@
  *  - grid_layout / assigned_grid2D / block<T>     src/grid2grid/grid_layout.hpp:7-63,
  *                                                 src/grid2grid/grid2D.hpp:46-125,
  *                                                 src/grid2grid/block.hpp:60-190
+ *  - communication_volume, optimal_reordering     src/grid2grid/transform.cpp:9-39,
+ *                                                 src/grid2grid/ranks_reordering.cpp:4-61
+ *  - get_scalapack_grid (as a ScaLAPACK front end) src/grid2grid/scalapack_layout.cpp:152-278
  */
 #ifndef GRID2GRID_GB300_H
 #define GRID2GRID_GB300_H
@@ -126,8 +129,8 @@ typedef struct g2g_tuning {
     int32_t tile_bytes;       /* target bytes per non-transposed tile       */
     int32_t tile_dim;         /* edge (elements) of a transposed tile: 16 or 32 */
     int32_t ctas_per_sm;      /* persistent grid = ctas_per_sm x SM count   */
-    int32_t threads;          /* threads per CTA: 128, 256 or 512           */
-    int32_t unroll;           /* 16-byte chunks in flight per thread: 1,2,4,8 */
+    int32_t threads;          /* threads per CTA: 256 or 512                */
+    int32_t unroll;           /* 16-byte chunks per lane and step: 1, 2 or 4 */
     int32_t stages;           /* plain copies: -1 = not TMA-staged,
                                  2..4 = TMA bulk copies into a ring of that
                                  many shared-memory stages (0 = default)    */
