@@ -79,7 +79,7 @@ class Tuning(C.Structure):
         ("unroll", C.c_int32),
         ("stages", C.c_int32),
         ("ring", C.c_int32),
-        ("reserved", C.c_int32),
+        ("tile_run", C.c_int32),
     ]
 
 

@@ -292,6 +292,7 @@ g2g_tuning default_tuning() {
     t.unroll = 4;
     t.stages = -1; // TMA staging is opt-in (no faster on measured workloads)
     t.ring = 1;
+    t.tile_run = 1;
     return t;
 }
 
@@ -306,6 +307,7 @@ g2g_tuning merge_tuning(const g2g_tuning &base, const g2g_tuning *over) {
     if (over->unroll) t.unroll = over->unroll;
     if (over->stages) t.stages = over->stages;
     if (over->ring) t.ring = over->ring;
+    if (over->tile_run) t.tile_run = over->tile_run;
     return t;
 }
 
@@ -323,6 +325,8 @@ g2g_status check_tuning(const g2g_tuning &t) {
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: stages must be -1 or 2..4");
     if (t.ring != -1 && t.ring != 1)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ring must be -1 or 1");
+    if (t.tile_run < 1 || t.tile_run > 64 || (t.tile_run & (t.tile_run - 1)))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_run must be a power of two in [1, 64]");
     if (t.ctas_per_sm < 1 || t.ctas_per_sm > 32)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ctas_per_sm outside [1, 32]");
     return G2G_SUCCESS;
@@ -698,6 +702,9 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     c.paths = pl.paths ? pl.paths : 1;
     // blocks in host memory take the register path: plain loads and stores
     c.ring = (pl.tuning.ring == 1 && !pl.host_memory) ? 1 : 0;
+    c.run_shift = 0;
+    while ((1 << c.run_shift) < pl.tuning.tile_run && c.run_shift < 6)
+        ++c.run_shift;
     c.stages = 0;
     if ((c.paths & 1) && pl.tuning.stages >= 2 && !pl.host_memory) {
         c.stage_bytes = g2g::stage_bytes_for(pl.tuning.tile_bytes);
@@ -1078,6 +1085,7 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
     const int ctas_opts[] = {2, 4, 8};
     const int stage_opts[] = {-1, 2, 3, 4};
     const int ring_opts[] = {1, -1};
+    const int run_opts[] = {1, 2};
     for (int tb : tile_bytes_opts)
         for (int td : tile_dim_opts) {
             if (!plan->any_trans && td != start.tile_dim)
@@ -1086,23 +1094,27 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
                 for (int u : unroll_opts)
                     for (int c : ctas_opts)
                         for (int sg : stage_opts)
-                            for (int rg : ring_opts) {
-                                if (th * c > 2048)
-                                    continue;
-                                if ((sg != -1 || rg != 1) && !(plan->paths & 1))
-                                    continue;
-                                if (sg != -1 && rg != 1)
-                                    continue;
-                                g2g_tuning t = start;
-                                t.tile_bytes = tb;
-                                t.tile_dim = td;
-                                t.threads = th;
-                                t.unroll = u;
-                                t.ctas_per_sm = c;
-                                t.stages = sg;
-                                t.ring = rg;
-                                cands.push_back(t);
-                            }
+                            for (int rg : ring_opts)
+                                for (int run : run_opts) {
+                                    if (th * c > 2048)
+                                        continue;
+                                    if ((sg != -1 || rg != 1) && !(plan->paths & 1))
+                                        continue;
+                                    if (sg != -1 && rg != 1)
+                                        continue;
+                                    if (run != 1 && (sg != -1 || rg != 1))
+                                        continue; // runs only matter to the ring
+                                    g2g_tuning t = start;
+                                    t.tile_bytes = tb;
+                                    t.tile_dim = td;
+                                    t.threads = th;
+                                    t.unroll = u;
+                                    t.ctas_per_sm = c;
+                                    t.stages = sg;
+                                    t.ring = rg;
+                                    t.tile_run = run;
+                                    cands.push_back(t);
+                                }
         }
     cudaEvent_t e0, e1;
     G2G_CUDA(cudaEventCreate(&e0));

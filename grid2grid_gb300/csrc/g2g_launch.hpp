@@ -67,6 +67,7 @@ struct ScatterConfig {
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
     int ring = 0;            // plain copies through the per-warp cp.async ring
+    int run_shift = 0;       // ring: runs of 2^run_shift consecutive tiles per warp
     int stage_bytes = 0;     // bytes per stage
     size_t trans_bytes = 0;  // shared memory for direct transposed / scaled tiles
 };

@@ -1477,6 +1477,19 @@ __device__ __forceinline__ void ring_queue_fetch(const PlanList &list, long long
     }
 }
 
+// Which copy tiles a warp takes: runs of 2^run_shift consecutive tiles, the
+// runs dealt round-robin over the grid's warps (one tile per run: plain
+// static striding). Consecutive tiles are neighbouring cells of a column
+// strip, so a run keeps one warp streaming along the same block columns.
+struct RingOrder {
+    long long base;   // first tile of the warp's first run
+    long long stride; // tiles between the starts of its runs
+    int shift;        // log2 of the run length
+};
+__device__ __forceinline__ long long tile_of(const RingOrder &o, int j) {
+    return o.base + (long long)(j >> o.shift) * o.stride + (j & ((1 << o.shift) - 1));
+}
+
 // The issuing side: its tile (index ti, ordinal j among the warp's tiles),
 // the tile's walk constants and this lane's position, the next chunk.
 struct RingIssue {
@@ -1489,29 +1502,30 @@ struct RingIssue {
 
 // Fills ring stage `st` from the issuing cursor (or marks it empty) and commits it.
 template <int U>
-__device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q, long long GW,
-                                          uint32_t slots, const unsigned char *queue,
-                                          uint32_t queue_s, int *valid, int lane) {
+__device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
+                                          const RingOrder &ord, uint32_t slots,
+                                          const unsigned char *queue, uint32_t queue_s,
+                                          int *valid, int lane) {
     if (q.ti < list.total_copy) {
         if (lane == 0)
             *valid = 1;
         ring_issue<U>(q.c, q.w, slots, lane);
         q.idx0 += 32 * U;
         if (q.idx0 >= q.c.total) { // on to the warp's next tile
-            q.ti += GW;
             ++q.j;
+            q.ti = tile_of(ord, q.j);
             q.idx0 = 0;
             if (q.ti < list.total_copy) {
                 ring_tile_init(q.c, *reinterpret_cast<const Tile *>(
                                         queue + (q.j & (RING_Q - 1)) * RING_QE));
                 ring_walk_init(q.w, q.c, lane);
-                ring_queue_fetch(list, q.ti + RING_LA * GW,
+                ring_queue_fetch(list, tile_of(ord, q.j + RING_LA),
                                  queue_s + (uint32_t)(((q.j + RING_LA) & (RING_Q - 1)) * RING_QE),
                                  lane);
-                if (lane == 0 && q.ti + (RING_LA + 2) * GW < list.total_copy) {
+                const long long pf = tile_of(ord, q.j + RING_LA + 2);
+                if (lane == 0 && pf < list.total_copy) {
                     const PairInfo *unused;
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(
-                        locate_copy(list, q.ti + (RING_LA + 2) * GW, unused)));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, pf, unused)));
                 }
             }
         }
@@ -1523,7 +1537,7 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q, lo
 
 template <int U>
 __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
-                                                int warp, int nwarp) {
+                                                int warp, int nwarp, int run_shift) {
     constexpr int SLOT_BYTES = ring_stage_bytes<U>();
     const int lane = threadIdx.x & 31;
     unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
@@ -1532,19 +1546,25 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     const uint32_t slots0 = smem_addr(wbase);
     const uint32_t queue_s = smem_addr(queue);
     const long long GW = (long long)gridDim.x * nwarp;
+    RingOrder ord;
+    ord.shift = run_shift;
+    ord.base = ((long long)blockIdx.x * nwarp + warp) << run_shift;
+    ord.stride = GW << run_shift;
     RingIssue q;
-    q.ti = (long long)blockIdx.x * nwarp + warp;
     q.j = 0;
+    q.ti = tile_of(ord, 0);
     q.idx0 = 0;
     // descriptors of the first RING_LA + 1 tiles, landed before the first fill
 #pragma unroll
     for (int k = 0; k <= RING_LA; ++k)
-        ring_queue_fetch(list, q.ti + k * GW, queue_s + (uint32_t)(k * RING_QE), lane);
+        ring_queue_fetch(list, tile_of(ord, k), queue_s + (uint32_t)(k * RING_QE), lane);
     cp_async_commit();
-    if (lane < 2 && q.ti + (RING_LA + 1 + lane) * GW < list.total_copy) {
-        const PairInfo *unused;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(
-            locate_copy(list, q.ti + (RING_LA + 1 + lane) * GW, unused)));
+    if (lane < 2) {
+        const long long pf = tile_of(ord, RING_LA + 1 + lane);
+        if (pf < list.total_copy) {
+            const PairInfo *unused;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, pf, unused)));
+        }
     }
     cp_async_wait<0>();
     __syncwarp();
@@ -1554,7 +1574,7 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     }
 #pragma unroll
     for (int st = 0; st < RING_D - 1; ++st)
-        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(st * SLOT_BYTES), queue, queue_s,
+        ring_fill<U>(list, q, ord, slots0 + (uint32_t)(st * SLOT_BYTES), queue, queue_s,
                      valid + st, lane);
     // the storing side: its tile ordinal, walk constants and position
     int js = -1;
@@ -1565,7 +1585,7 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     int sp = 0; // stage to store; the stage before it is filled next
     for (;;) {
         const int sf = sp == 0 ? RING_D - 1 : sp - 1;
-        ring_fill<U>(list, q, GW, slots0 + (uint32_t)(sf * SLOT_BYTES), queue, queue_s,
+        ring_fill<U>(list, q, ord, slots0 + (uint32_t)(sf * SLOT_BYTES), queue, queue_s,
                      valid + sf, lane);
         cp_async_wait<RING_D - 1>();
         __syncwarp();
@@ -1596,10 +1616,10 @@ template <int THREADS, int PATHS> struct RingMinBlocks {
 
 template <int THREADS, int U, int PATHS>
 __global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS, PATHS>::value))
-    scatter_ring_kernel(const __grid_constant__ PlanList list, int td) {
+    scatter_ring_kernel(const __grid_constant__ PlanList list, int td, int run_shift) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;
-    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP);
+    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP, run_shift);
     if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
         __syncthreads(); // the ring's shared memory becomes the CTA tiles'
         cta_phase<THREADS, PATHS>(list, smem, td);
@@ -1713,7 +1733,7 @@ cudaError_t launch_ring(const PlanList &list, const ScatterConfig &cfg, cudaStre
     cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
     if (e != cudaSuccess)
         return e;
-    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim);
+    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim, cfg.run_shift);
     return cudaGetLastError();
 }
 

@@ -137,7 +137,8 @@ typedef struct g2g_tuning {
     int32_t ring;             /* plain copies when not TMA-staged: 1 = per-warp
                                  cp.async ring in shared memory, -1 = loads
                                  through registers (0 = default)            */
-    int32_t reserved;
+    int32_t tile_run;         /* ring: a warp takes runs of this many
+                                 consecutive tiles (1, 2, 4 .. 64; 0 = default) */
 } g2g_tuning;
 
 typedef struct g2g_plan_info {

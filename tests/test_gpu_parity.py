@@ -169,7 +169,8 @@ def test_mixed_dtype_batch_matches_port():
     dict(tile_bytes=65536, tile_dim=32, ctas_per_sm=1, threads=512),
     dict(threads=256, unroll=1, ring=-1), dict(threads=512, unroll=4, ring=-1),
     dict(threads=256, unroll=2, ring=1), dict(threads=512, unroll=1, ring=1),
-    dict(tile_bytes=512, unroll=4, ring=1, ctas_per_sm=1)])
+    dict(tile_bytes=512, unroll=4, ring=1, ctas_per_sm=1),
+    dict(tile_bytes=2048, ring=1, tile_run=8), dict(threads=256, ring=1, tile_run=64)])
 def test_tunings_give_identical_results(tuning):
     rng = np.random.default_rng(77)
     inits, finals, ias, fas, ops = [], [], [], [], []
