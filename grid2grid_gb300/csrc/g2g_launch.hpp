@@ -79,6 +79,11 @@ int stage_bytes_for(int tile_bytes);
 size_t staged_smem_bytes(const ScatterConfig &cfg);
 // Dynamic shared memory of the ring kernel.
 size_t ring_smem_bytes(const ScatterConfig &cfg);
+// Resident CTAs per SM of kernel `fn` at `threads` threads and `smem` bytes
+// of dynamic shared memory on the current device; sets the kernel's shared
+// memory limit first when it is above the default. Computed once per
+// (device, kernel, threads, smem) and cached: launches pay a table lookup.
+cudaError_t kernel_occupancy(const void *fn, int threads, size_t smem, int *occ);
 // The kernel instances by CTA size (one translation unit each).
 cudaError_t launch_scatter_256(const PlanList &list, const ScatterConfig &cfg,
                                cudaStream_t stream);

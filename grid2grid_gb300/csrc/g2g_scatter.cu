@@ -3,7 +3,44 @@
 // units (g2g_scatter_256.cu, g2g_scatter_512.cu) so they compile in parallel.
 #include "g2g_scatter_impl.cuh"
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 namespace g2g {
+
+cudaError_t kernel_occupancy(const void *fn, int threads, size_t smem, int *occ) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void *, int, size_t>, int> cache;
+    static std::map<std::pair<int, const void *>, size_t> smem_limit; // as set so far
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess)
+        return e;
+    const auto key = std::make_tuple(device, fn, threads, smem);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        *occ = it->second;
+        return cudaSuccess;
+    }
+    // the limit only ever grows, so every size cached for this kernel stays
+    // launchable
+    size_t &limit = smem_limit[std::make_pair(device, fn)];
+    if (smem > 48 * 1024 && smem > limit) {
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        limit = smem;
+    }
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem);
+    if (e != cudaSuccess)
+        return e;
+    cache[key] = n;
+    *occ = n;
+    return cudaSuccess;
+}
 
 size_t transpose_smem_bytes(int tile_dim, int esz) {
     return (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;

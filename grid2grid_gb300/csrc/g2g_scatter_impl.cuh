@@ -1690,14 +1690,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 template <typename K>
 cudaError_t prepare(K k, const ScatterConfig &cfg, size_t smem, long long total,
                     unsigned &grid_out) {
-    if (smem > 48 * 1024) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-    }
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, cfg.threads, smem);
+    cudaError_t e = kernel_occupancy((const void *)k, cfg.threads, smem, &occ);
     if (e != cudaSuccess)
         return e;
     if (occ < 1)
