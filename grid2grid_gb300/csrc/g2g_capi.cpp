@@ -350,7 +350,8 @@ struct g2g_plan {
     int64_t bytes_moved = 0, bytes_min_traffic = 0;
     bool any_trans = false;
     int max_trans_esz = 0;
-    int paths = 0; // tile paths the work list needs (1 copy, 2 transpose, 4 scaled)
+    int paths = 0; // tile paths the work list needs (1 copy, 2 transpose,
+                   // 4 scaled real, 8 scaled complex)
     bool host_memory = false; // some block lives in pinned host memory
     g2g_tuning tuning;
     // device
@@ -525,8 +526,8 @@ void assemble(g2g_plan &pl) {
         for (const HBlock &b : p.a.blocks)
             if (!b.trans)
                 any_plain = true;
-        if (p.scaled)
-            pl.paths |= 4;
+        if (p.scaled) // real and complex arithmetic are separate kernel paths
+            pl.paths |= (p.dtype == G2G_COMPLEX64 || p.dtype == G2G_COMPLEX128) ? 8 : 4;
         else
             pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0);
     }

@@ -64,7 +64,8 @@ struct ScatterConfig {
     int sm_count = 0;        // for the residency clamp of the persistent grid
     int tile_dim = 32;       // transposed tile edge (16 or 32)
     size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
-    int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled
+    int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled real,
+                             // 8 scaled complex
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
     int ring = 0;            // plain copies through the per-warp cp.async ring
     int run_shift = 0;       // ring: runs of 2^run_shift consecutive tiles per warp

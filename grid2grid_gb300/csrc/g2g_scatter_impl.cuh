@@ -40,6 +40,17 @@ namespace g2g {
 
 namespace {
 
+// Tile paths a kernel instance contains; a plan launches the smallest
+// instance that covers its tiles, so the plain copy does not carry the
+// register cost of the scaled complex arithmetic.
+enum : int {
+    PATH_COPY = 1,
+    PATH_TRANSPOSE = 2,
+    PATH_SCALED_REAL = 4,    // scaled float / double tiles
+    PATH_SCALED_COMPLEX = 8, // scaled complex tiles (more registers)
+    PATH_SCALED = PATH_SCALED_REAL | PATH_SCALED_COMPLEX
+};
+
 // ---------------------------------------------------------------- memory ops
 __device__ __forceinline__ uint4 ldg_v4(uint64_t addr) {
     uint4 v;
@@ -1161,43 +1172,68 @@ __device__ __forceinline__ void scaled_transpose_store(const Tile &t, const Pair
 }
 
 // ------------------------------------------------------------------ kernel
-template <int THREADS>
+// (a kernel carries the arithmetic of the element types its plan scales:
+// real, complex or both)
+template <int THREADS, int PATHS>
 __device__ __forceinline__ void scaled_dispatch(const Tile &t, const PairInfo *pairs,
                                                 unsigned char *smem, int td) {
     switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
-    case 0: scaled_tile<THREADS, float>(t, pairs, smem, td); break;
-    case 1: scaled_tile<THREADS, double>(t, pairs, smem, td); break;
-    case 2: scaled_tile<THREADS, cplxf>(t, pairs, smem, td); break;
-    default: scaled_tile<THREADS, cplxd>(t, pairs, smem, td); break;
+    case 0:
+        if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+            scaled_tile<THREADS, float>(t, pairs, smem, td);
+        break;
+    case 1:
+        if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+            scaled_tile<THREADS, double>(t, pairs, smem, td);
+        break;
+    case 2:
+        if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+            scaled_tile<THREADS, cplxf>(t, pairs, smem, td);
+        break;
+    default:
+        if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+            scaled_tile<THREADS, cplxd>(t, pairs, smem, td);
+        break;
     }
 }
-template <int THREADS>
+template <int THREADS, int PATHS>
 __device__ __forceinline__ void scaled_transpose_dispatch(const Tile &t, const PairInfo *pairs,
                                                           const unsigned char *smem, int td) {
     switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
-    case 0: scaled_transpose_store<THREADS, float>(t, pairs, smem, td); break;
-    case 1: scaled_transpose_store<THREADS, double>(t, pairs, smem, td); break;
-    case 2: scaled_transpose_store<THREADS, cplxf>(t, pairs, smem, td); break;
-    default: scaled_transpose_store<THREADS, cplxd>(t, pairs, smem, td); break;
+    case 0:
+        if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+            scaled_transpose_store<THREADS, float>(t, pairs, smem, td);
+        break;
+    case 1:
+        if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+            scaled_transpose_store<THREADS, double>(t, pairs, smem, td);
+        break;
+    case 2:
+        if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+            scaled_transpose_store<THREADS, cplxf>(t, pairs, smem, td);
+        break;
+    default:
+        if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+            scaled_transpose_store<THREADS, cplxd>(t, pairs, smem, td);
+        break;
     }
 }
 
-// Tile paths a kernel instance contains; a plan launches the smallest
-// instance that covers its tiles, so the plain copy does not carry the
-// register cost of the scaled complex arithmetic.
-enum : int { PATH_COPY = 1, PATH_TRANSPOSE = 2, PATH_SCALED = 4 };
+
 
 // Register budget: 64 per thread (1024 resident threads per SM), enough for
 // U = 4 chunks per lane in flight on the register path without spilling.
 template <int U, int THREADS> struct MinBlocks {
     static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
 };
-// Kernels with scaled tiles: 128 registers (512 resident threads per SM),
-// room for the complex arithmetic of the scaled paths without spilling.
+// Kernels with scaled tiles: 128 registers (512 resident threads per SM)
+// for the complex arithmetic, 80 (768 threads) for the real one, so that
+// neither spills.
 template <int PATHS, int U, int THREADS> struct MinBlocksP {
-    static constexpr int value = (PATHS & PATH_SCALED)
-                                     ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
-                                     : MinBlocks<U, THREADS>::value;
+    static constexpr int value =
+        (PATHS & PATH_SCALED_COMPLEX) ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
+        : (PATHS & PATH_SCALED_REAL)  ? ((768 / THREADS) > 0 ? (768 / THREADS) : 1)
+                                      : MinBlocks<U, THREADS>::value;
 };
 
 // CTA-level tiles (transposed, scaled) of a launch, static striding, with the
@@ -1246,12 +1282,12 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
             if (PIPE && next < n && is_plain_transpose(nxt))
                 load_tile_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
             if ((PATHS & PATH_SCALED) && (cur.kind & KIND_SCALED))
-                scaled_transpose_dispatch<THREADS>(cur, cur_pairs, smem, td);
+                scaled_transpose_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             else
                 smem_to_global<THREADS, NE>(cur, td_shift, smem);
         } else {
             if (PATHS & PATH_SCALED)
-                scaled_dispatch<THREADS>(cur, cur_pairs, smem, td);
+                scaled_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             if (PIPE && next < n && is_plain_transpose(nxt))
                 load_tile_slots<THREADS, NE>(nxt, td_shift, v);
         }
@@ -1609,7 +1645,7 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
 // Registers: the ring kernel runs 16 warps per SM on copy-only plans (one
 // 512-thread CTA, or two of 256), 24 with CTA-level tiles (three of 256).
 template <int THREADS, int PATHS> struct RingMinBlocks {
-    static constexpr int value = (PATHS & PATH_SCALED)
+    static constexpr int value = (PATHS & PATH_SCALED_COMPLEX)
                                      ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
                                      : ((768 / THREADS) > 0 ? (768 / THREADS) : 1);
 };
@@ -1764,8 +1800,10 @@ cudaError_t launch_u(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s
 
 template <int THREADS>
 cudaError_t launch_p(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
-    if (cfg.paths & PATH_SCALED)
+    if (cfg.paths & PATH_SCALED_COMPLEX)
         return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(l, cfg, s);
+    if (cfg.paths & PATH_SCALED_REAL)
+        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED_REAL>(l, cfg, s);
     if (cfg.paths == PATH_COPY)
         return launch_u<THREADS, PATH_COPY>(l, cfg, s);
     if (cfg.paths == PATH_TRANSPOSE)
