@@ -164,6 +164,11 @@ SIGNATURES = [
     ("g2g_plan_create_batch", C.c_int,
      [C.c_int32, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.POINTER(C.c_int),
       C.POINTER(Op), _VP, C.POINTER(_VP)]),
+    ("g2g_plan_create_cast", C.c_int,
+     [C.POINTER(LayoutDesc), C.c_int, C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op), _VP,
+      C.POINTER(_VP)]),
+    ("g2g_transform_cast", C.c_int,
+     [C.POINTER(LayoutDesc), C.c_int, C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op), _VP]),
     ("g2g_plan_execute", C.c_int, [_VP, _VP]),
     ("g2g_plans_execute", C.c_int, [C.c_int32, C.POINTER(_VP), _VP]),
     ("g2g_plan_capture_graph", C.c_int, [_VP, _VP]),

@@ -274,8 +274,11 @@ void transpose_layout(HLayout &L, char flag) {
 // ------------------------------------------------------------------- plans
 struct PairHost {
     HLayout a, b; // a: initial after op, b: final
-    int dtype = 0;
+    int dtype = 0;     // the final layout's element type
     int esz = 0;
+    int src_dtype = 0; // the initial layout's (another one: a fused cast)
+    int src_esz = 0;
+    bool cast = false;
     bool scaled = false;
     bool any_trans = false;
     double alpha[2] = {1, 0}, beta[2] = {0, 0};
@@ -351,7 +354,7 @@ struct g2g_plan {
     bool any_trans = false;
     int max_trans_esz = 0;
     int paths = 0; // tile paths the work list needs (1 copy, 2 transpose,
-                   // 4 scaled real, 8 scaled complex)
+                   // 4 scaled real, 8 scaled complex, 16 cast)
     bool host_memory = false; // some block lives in pinned host memory
     g2g_tuning tuning;
     // device
@@ -392,20 +395,36 @@ int64_t tile_capacity_bound(const PairHost &p, const g2g_tuning &t) {
     return bound;
 }
 
+// A fused cast converts float <-> double, complex<float> <-> complex<double>
+// (each part) and real -> complex (imaginary part +0).
+bool cast_supported(int from, int to) {
+    const bool fc = dtype_complex(from), tc = dtype_complex(to);
+    return from != to && !(fc && !tc);
+}
+
 g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int dtype,
-                      const g2g_op *op, int pair_index, PairHost &p) {
+                      const g2g_op *op, int pair_index, PairHost &p, int src_dtype = -1) {
     (void)pair_index;
     p.dtype = dtype;
     p.esz = dtype_esz(dtype);
     if (!p.esz)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "unknown dtype %d", dtype);
+    p.src_dtype = src_dtype < 0 ? dtype : src_dtype;
+    p.src_esz = dtype_esz(p.src_dtype);
+    if (!p.src_esz)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "unknown source dtype %d", p.src_dtype);
+    p.cast = p.src_dtype != dtype;
+    if (p.cast && !cast_supported(p.src_dtype, dtype))
+        return fail(G2G_ERROR_UNSUPPORTED,
+                    "cast from dtype %d to dtype %d is not supported (complex to real)",
+                    p.src_dtype, dtype);
     if (!di || !df)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "layout descriptor is NULL");
     const int P = std::max(1, std::max(di->n_ranks, df->n_ranks));
     // element alignment: that of the real component (float or double)
-    const int align = (dtype == G2G_FLOAT32 || dtype == G2G_COMPLEX64) ? 4 : 8;
-    G2G_TRY(load_layout(di, "initial", P, false, align, p.a));
-    G2G_TRY(load_layout(df, "final", P, true, align, p.b));
+    auto comp_align = [](int dt) { return (dt == G2G_FLOAT32 || dt == G2G_COMPLEX64) ? 4 : 8; };
+    G2G_TRY(load_layout(di, "initial", P, false, comp_align(p.src_dtype), p.a));
+    G2G_TRY(load_layout(df, "final", P, true, comp_align(dtype), p.b));
     char trans = 'N';
     if (op) {
         trans = (char)std::toupper((unsigned char)op->trans);
@@ -438,6 +457,8 @@ g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int 
         p.scaled = !(p.alpha[0] == 1.0 && p.alpha[1] == 0.0 && p.beta[0] == 0.0 &&
                      p.beta[1] == 0.0);
     }
+    if (p.cast && p.scaled)
+        return fail(G2G_ERROR_UNSUPPORTED, "a cast transform takes alpha = 1, beta = 0");
     for (const HBlock &b : p.a.blocks)
         if (b.trans)
             p.any_trans = true;
@@ -501,7 +522,10 @@ void assemble(g2g_plan &pl) {
         pl.n_cells += cells;
         pl.max_cells_per_pair = std::max(pl.max_cells_per_pair, cells);
         pi.kind = esz_code(p.esz) | ((uint32_t)p.dtype << g2g::KIND_DTYPE_SHIFT) |
-                  (p.scaled ? g2g::KIND_SCALED : 0u);
+                  (p.scaled ? g2g::KIND_SCALED : 0u) |
+                  (p.cast ? (g2g::KIND_CAST |
+                             ((uint32_t)p.src_dtype << g2g::KIND_SRC_DTYPE_SHIFT))
+                          : 0u);
         pi.tile_rows = (int32_t)std::max(1, 4096 / p.esz);
         pi.tile_bytes = pl.tuning.tile_bytes;
         pi.tile_dim = pl.tuning.tile_dim;
@@ -517,7 +541,8 @@ void assemble(g2g_plan &pl) {
         pi.beta[1] = p.beta[1];
         const int64_t bytes = p.m * p.n * p.esz;
         pl.bytes_moved += bytes;
-        pl.bytes_min_traffic += (p.scaled ? 3 : 2) * bytes;
+        pl.bytes_min_traffic += p.cast ? p.m * p.n * (p.src_esz + p.esz)
+                                       : (p.scaled ? 3 : 2) * bytes;
         if (p.any_trans) {
             pl.any_trans = true;
             pl.max_trans_esz = std::max(pl.max_trans_esz, p.esz);
@@ -526,7 +551,9 @@ void assemble(g2g_plan &pl) {
         for (const HBlock &b : p.a.blocks)
             if (!b.trans)
                 any_plain = true;
-        if (p.scaled) // real and complex arithmetic are separate kernel paths
+        if (p.cast)
+            pl.paths |= 16;
+        else if (p.scaled) // real and complex arithmetic are separate kernel paths
             pl.paths |= (p.dtype == G2G_COMPLEX64 || p.dtype == G2G_COMPLEX128) ? 8 : 4;
         else
             pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0);
@@ -771,7 +798,7 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
 
 g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layout_desc *finals,
                        const g2g_dtype *dtypes, g2g_dtype single_dtype, const g2g_op *ops,
-                       g2g_plan **out) {
+                       g2g_plan **out, int src_dtype = -1) {
     if (!out)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "plan output pointer is NULL");
     *out = nullptr;
@@ -786,7 +813,7 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
     for (int k = 0; k < n_pairs; ++k) {
         int dt = dtypes ? (int)dtypes[k] : (int)single_dtype;
         g2g_status st = build_pair(&inits[k], &finals[k], dt, ops ? &ops[k] : nullptr, k,
-                                   pl->host[k]);
+                                   pl->host[k], src_dtype);
         if (st != G2G_SUCCESS) {
             if (n_pairs > 1)
                 t_last_error = "pair " + std::to_string(k) + ": " + t_last_error;
@@ -962,6 +989,28 @@ g2g_status g2g_plan_create(const g2g_layout_desc *initial, const g2g_layout_desc
                            g2g_plan **plan) {
     (void)stream;
     return create_plan(1, initial, final_, nullptr, dtype, op, plan);
+}
+
+g2g_status g2g_plan_create_cast(const g2g_layout_desc *initial, g2g_dtype src_dtype,
+                                const g2g_layout_desc *final_, g2g_dtype dst_dtype,
+                                const g2g_op *op, void *stream, g2g_plan **plan) {
+    (void)stream;
+    return create_plan(1, initial, final_, nullptr, dst_dtype, op, plan, (int)src_dtype);
+}
+
+g2g_status g2g_transform_cast(const g2g_layout_desc *initial, g2g_dtype src_dtype,
+                              const g2g_layout_desc *final_, g2g_dtype dst_dtype,
+                              const g2g_op *op, void *stream) {
+    g2g_plan *plan = nullptr;
+    G2G_TRY(g2g_plan_create_cast(initial, src_dtype, final_, dst_dtype, op, stream, &plan));
+    g2g_status st = g2g_plan_execute(plan, stream);
+    if (st == G2G_SUCCESS) {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        if (e != cudaSuccess)
+            st = fail(G2G_ERROR_CUDA, "cast transform failed: %s", cudaGetErrorString(e));
+    }
+    g2g_status st2 = g2g_plan_destroy(plan);
+    return st != G2G_SUCCESS ? st : st2;
 }
 
 g2g_status g2g_plan_create_batch(int32_t n_pairs, const g2g_layout_desc *initials,

@@ -25,10 +25,19 @@ enum : uint32_t {
     KIND_TRANS = 0x4u,      // source is read transposed
     KIND_CONJ = 0x8u,       // flip the sign of the imaginary part
     KIND_SCALED = 0x10u,    // dst = beta*dst + alpha*src instead of a copy
-    KIND_DTYPE_SHIFT = 8u,  // g2g_dtype in bits 8-9
+    KIND_CAST = 0x20u,      // source elements of another type, converted
+    KIND_DTYPE_SHIFT = 8u,  // g2g_dtype in bits 8-9 (the destination's)
+    KIND_SRC_DTYPE_SHIFT = 10u, // with KIND_CAST: the source's g2g_dtype, bits 10-11
 };
 
 __host__ __device__ inline int kind_esz(uint32_t kind) { return 4 << (kind & KIND_ESZ_MASK); }
+// Bytes of a source element: the destination's unless the tile converts.
+__host__ __device__ inline int kind_src_esz(uint32_t kind) {
+    if (!(kind & KIND_CAST))
+        return kind_esz(kind);
+    const uint32_t dt = (kind >> KIND_SRC_DTYPE_SHIFT) & 3u; // 0 f32, 1 f64, 2 c64, 3 c128
+    return dt == 0 ? 4 : (dt == 3 ? 16 : 8);
+}
 
 // One entry of the dense initial block table: where block (i, j) of the
 // (transposed) initial grid lives. The table has one entry per grid block.

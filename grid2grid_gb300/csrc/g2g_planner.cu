@@ -123,7 +123,7 @@ __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
 // Plain copies are warp-level work items, transposed and scaled tiles
 // CTA-level ones; the work list holds all copy tiles first.
 __device__ inline bool is_copy_kind(uint32_t kind) {
-    return !(kind & (KIND_TRANS | KIND_SCALED));
+    return !(kind & (KIND_TRANS | KIND_SCALED | KIND_CAST));
 }
 
 __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pairs,
@@ -285,7 +285,7 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
         const DstEntry de = dst_tables[p.dst_table + (long long)pr.ib * p.b_nc + pc.ib];
         const bool trans = (se.flags & 1u) != 0;
         uint32_t kind = p.kind | (trans ? KIND_TRANS : 0u) | ((se.flags & 2u) ? KIND_CONJ : 0u);
-        const int esz = kind_esz(kind);
+        const int esz = kind_esz(kind), sesz = kind_src_esz(kind);
         int tr, tc;
         tile_shape(p, kind, pr.len, pc.len, tr, tc);
         const int ntr = (pr.len + tr - 1) / tr;
@@ -313,9 +313,9 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
             Tile T;
             long long rr = sr + r0, cc = sc + c0;
             long long src_off = trans ? (rr * se.ld + cc) : (rr + cc * se.ld);
-            T.src = se.data + (uint64_t)(src_off * esz);
+            T.src = se.data + (uint64_t)(src_off * sesz);
             T.dst = de.data + (uint64_t)(((dr + r0) + (dc + c0) * de.ld) * esz);
-            T.src_ld = se.ld * esz;
+            T.src_ld = se.ld * sesz;
             T.dst_ld = de.ld * esz;
             T.rows = (int)((pr.len - r0) < tr ? (pr.len - r0) : tr);
             T.cols = (int)((pc.len - c0) < tc ? (pc.len - c0) : tc);

@@ -48,7 +48,8 @@ enum : int {
     PATH_TRANSPOSE = 2,
     PATH_SCALED_REAL = 4,    // scaled float / double tiles
     PATH_SCALED_COMPLEX = 8, // scaled complex tiles (more registers)
-    PATH_SCALED = PATH_SCALED_REAL | PATH_SCALED_COMPLEX
+    PATH_SCALED = PATH_SCALED_REAL | PATH_SCALED_COMPLEX,
+    PATH_CAST = 16           // tiles converting the element type
 };
 
 // ---------------------------------------------------------------- memory ops
@@ -1171,6 +1172,109 @@ __device__ __forceinline__ void scaled_transpose_store(const Tile &t, const Pair
     }
 }
 
+// -------------------------------------------------------------- cast tiles
+// A fused cast: final = convert(op(initial)). float <-> double and
+// complex<float> <-> complex<double> round each part to nearest (the CUDA
+// conversion intrinsics, IEEE round-to-nearest-even); real -> complex sets
+// the imaginary part to +0; 'C' flips the imaginary sign after the
+// conversion. CTA-wide: non-transposed tiles walk columns (warps) and rows
+// (lanes, four elements in flight each); transposed ones go through a padded
+// shared-memory tile of destination elements.
+__device__ __forceinline__ float cvt(float v, float *) { return v; }
+__device__ __forceinline__ double cvt(float v, double *) { return (double)v; }
+__device__ __forceinline__ float cvt(double v, float *) { return __double2float_rn(v); }
+__device__ __forceinline__ double cvt(double v, double *) { return v; }
+__device__ __forceinline__ cplxf cvt(float v, cplxf *) { return cplxf{v, 0.0f}; }
+__device__ __forceinline__ cplxd cvt(float v, cplxd *) { return cplxd{(double)v, 0.0}; }
+__device__ __forceinline__ cplxf cvt(double v, cplxf *) {
+    return cplxf{__double2float_rn(v), 0.0f};
+}
+__device__ __forceinline__ cplxd cvt(double v, cplxd *) { return cplxd{v, 0.0}; }
+__device__ __forceinline__ cplxf cvt(cplxf v, cplxf *) { return v; }
+__device__ __forceinline__ cplxd cvt(cplxf v, cplxd *) { return cplxd{(double)v.x, (double)v.y}; }
+__device__ __forceinline__ cplxf cvt(cplxd v, cplxf *) {
+    return cplxf{__double2float_rn(v.x), __double2float_rn(v.y)};
+}
+__device__ __forceinline__ cplxd cvt(cplxd v, cplxd *) { return v; }
+template <typename D, typename S> __device__ __forceinline__ D convert(S v) {
+    return cvt(v, (D *)nullptr);
+}
+
+// (one function per conversion, called per tile: the kernel does not carry
+// the registers of all twelve)
+template <int THREADS, typename S, typename D>
+__device__ __noinline__ void cast_tile(const Tile &t, unsigned char *smem_raw, int td) {
+    constexpr int NWARP = THREADS / 32;
+    constexpr int ES = (int)sizeof(S), ED = (int)sizeof(D);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    const int R = t.rows, Cn = t.cols;
+    if (!(t.kind & KIND_TRANS)) {
+        for (int c = warp; c < Cn; c += NWARP) {
+            const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
+            const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+            for (int r0 = lane; r0 < R; r0 += 32 * 4) {
+                S v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (r0 + 32 * k < R)
+                        v[k] = ld_elem<S>(sc + (uint64_t)(r0 + 32 * k) * ES);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (r0 + 32 * k < R)
+                        st_elem<D>(dc + (uint64_t)(r0 + 32 * k) * ED, convert<D>(v[k]));
+            }
+        }
+        return;
+    }
+    D *smem = reinterpret_cast<D *>(smem_raw);
+    const int pitch = td + 1;
+    __syncthreads(); // earlier tiles are out of shared memory
+    for (int r = warp; r < R; r += NWARP)
+        for (int c = lane; c < Cn; c += 32)
+            smem[r * pitch + c] = convert<D>(
+                ld_elem<S>(t.src + (uint64_t)((long long)r * t.src_ld + (long long)c * ES)));
+    __syncthreads();
+    for (int c = warp; c < Cn; c += NWARP) {
+        const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+        for (int r = lane; r < R; r += 32) {
+            D v = smem[r * pitch + c];
+            if (conj)
+                v = conj_elem(v);
+            st_elem<D>(dc + (uint64_t)r * ED, v);
+        }
+    }
+}
+
+template <typename T> struct is_cplx { static constexpr bool value = false; };
+template <> struct is_cplx<cplxf> { static constexpr bool value = true; };
+template <> struct is_cplx<cplxd> { static constexpr bool value = true; };
+
+template <int THREADS, typename S>
+__device__ __forceinline__ void cast_to(const Tile &t, unsigned char *smem, int td) {
+    switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0: // complex -> real is refused on the host
+        if constexpr (!is_cplx<S>::value)
+            cast_tile<THREADS, S, float>(t, smem, td);
+        break;
+    case 1:
+        if constexpr (!is_cplx<S>::value)
+            cast_tile<THREADS, S, double>(t, smem, td);
+        break;
+    case 2: cast_tile<THREADS, S, cplxf>(t, smem, td); break;
+    default: cast_tile<THREADS, S, cplxd>(t, smem, td); break;
+    }
+}
+template <int THREADS>
+__device__ __forceinline__ void cast_dispatch(const Tile &t, unsigned char *smem, int td) {
+    switch ((t.kind >> KIND_SRC_DTYPE_SHIFT) & 3u) {
+    case 0: cast_to<THREADS, float>(t, smem, td); break;
+    case 1: cast_to<THREADS, double>(t, smem, td); break;
+    case 2: cast_to<THREADS, cplxf>(t, smem, td); break;
+    default: cast_to<THREADS, cplxd>(t, smem, td); break;
+    }
+}
+
 // ------------------------------------------------------------------ kernel
 // (a kernel carries the arithmetic of the element types its plan scales:
 // real, complex or both)
@@ -1227,11 +1331,11 @@ template <int U, int THREADS> struct MinBlocks {
     static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
 };
 // Kernels with scaled tiles: 128 registers (512 resident threads per SM)
-// for the complex arithmetic, 80 (768 threads) for the real one, so that
-// neither spills.
+// for the complex arithmetic (and the element conversions of cast tiles),
+// 80 (768 threads) for the real one, so that neither spills.
 template <int PATHS, int U, int THREADS> struct MinBlocksP {
     static constexpr int value =
-        (PATHS & PATH_SCALED_COMPLEX) ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
+        (PATHS & (PATH_SCALED_COMPLEX | PATH_CAST)) ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
         : (PATHS & PATH_SCALED_REAL)  ? ((768 / THREADS) > 0 ? (768 / THREADS) : 1)
                                       : MinBlocks<U, THREADS>::value;
 };
@@ -1241,10 +1345,10 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
 template <int THREADS, int PATHS>
 __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
     constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
-    // Kernels with scaled tiles move plain transposed tiles one at a time:
-    // the next tile's loads held across the scaled arithmetic would cost
+    // Kernels with scaled or cast tiles move plain transposed tiles one at a
+    // time: the next tile's loads held across their element code would cost
     // more registers than the overlap gains.
-    constexpr bool PIPE = (PATHS & PATH_TRANSPOSE) && !(PATHS & PATH_SCALED);
+    constexpr bool PIPE = (PATHS & PATH_TRANSPOSE) && !(PATHS & (PATH_SCALED | PATH_CAST));
     const int td_shift = td >= 32 ? 5 : 4;
     const long long n = list.total_cta;
     const long long G = gridDim.x;
@@ -1270,8 +1374,9 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_cta(list, next + G, unused)));
             }
         }
-        const bool staged = (PATHS & PATH_SCALED) ? (cur.kind & KIND_TRANS) != 0
-                                                  : is_plain_transpose(cur);
+        const bool staged = !(cur.kind & KIND_CAST) &&
+                            ((PATHS & PATH_SCALED) ? (cur.kind & KIND_TRANS) != 0
+                                                   : is_plain_transpose(cur));
         if ((PATHS & (PATH_TRANSPOSE | PATH_SCALED)) && staged) {
             __syncthreads(); // earlier tiles are out of shared memory
             // transposed tiles, plain or scaled, staged through shared memory
@@ -1286,7 +1391,9 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
             else
                 smem_to_global<THREADS, NE>(cur, td_shift, smem);
         } else {
-            if (PATHS & PATH_SCALED)
+            if ((PATHS & PATH_CAST) && (cur.kind & KIND_CAST))
+                cast_dispatch<THREADS>(cur, smem, td);
+            else if (PATHS & PATH_SCALED)
                 scaled_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             if (PIPE && next < n && is_plain_transpose(nxt))
                 load_tile_slots<THREADS, NE>(nxt, td_shift, v);
@@ -1321,7 +1428,7 @@ __global__ void __launch_bounds__(THREADS, (MinBlocksP<PATHS, U, THREADS>::value
         }
     }
     // phase 2: transposed and scaled tiles, one CTA per tile
-    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED | PATH_CAST))
         cta_phase<THREADS, PATHS>(list, smem, td);
 }
 
@@ -1645,7 +1752,7 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
 // Registers: the ring kernel runs 16 warps per SM on copy-only plans (one
 // 512-thread CTA, or two of 256), 24 with CTA-level tiles (three of 256).
 template <int THREADS, int PATHS> struct RingMinBlocks {
-    static constexpr int value = (PATHS & PATH_SCALED_COMPLEX)
+    static constexpr int value = (PATHS & (PATH_SCALED_COMPLEX | PATH_CAST))
                                      ? ((512 / THREADS) > 0 ? (512 / THREADS) : 1)
                                      : ((768 / THREADS) > 0 ? (768 / THREADS) : 1);
 };
@@ -1656,7 +1763,7 @@ __global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS, PATHS>::value
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;
     ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP, run_shift);
-    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED)) {
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED | PATH_CAST)) {
         __syncthreads(); // the ring's shared memory becomes the CTA tiles'
         cta_phase<THREADS, PATHS>(list, smem, td);
     }
@@ -1719,7 +1826,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             issue_stage(list, ti + (long long)S * G, n, stage, bar, stage_bytes);
         st = (st + 1 == S) ? 0 : st + 1;
     }
-    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED))
+    if (PATHS & (PATH_TRANSPOSE | PATH_SCALED | PATH_CAST))
         cta_phase<THREADS, PATHS>(list, direct, td);
 }
 
@@ -1800,6 +1907,11 @@ cudaError_t launch_u(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s
 
 template <int THREADS>
 cudaError_t launch_p(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
+    if (cfg.paths & PATH_CAST) {
+        if (cfg.paths & PATH_SCALED) // not generated: cast and scaled plans launch apart
+            return cudaErrorNotSupported;
+        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_CAST>(l, cfg, s);
+    }
     if (cfg.paths & PATH_SCALED_COMPLEX)
         return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(l, cfg, s);
     if (cfg.paths & PATH_SCALED_REAL)

@@ -213,6 +213,25 @@ g2g_status g2g_plan_get_info(const g2g_plan *plan, g2g_plan_info *info);
  * stream has finished (stream-ordered free). */
 g2g_status g2g_plan_destroy(g2g_plan *plan);
 
+/* ---- fused dtype cast (beyond the reference) --------------------------- */
+
+/* A transform that converts the element type on the way:
+ * final = convert(op(initial)), the initial layout holding src_dtype
+ * elements and the final one dst_dtype elements. Supported: float <-> double
+ * and complex<float> <-> complex<double> (each part rounded to nearest even),
+ * real -> complex (imaginary part +0); complex -> real is
+ * G2G_ERROR_UNSUPPORTED. op: trans 'N', 'T' or 'C' ('C' conjugates after the
+ * conversion); alpha and beta must be 1 and 0 (op may be NULL). The reference
+ * has no such operation; results are checked against numpy's conversions. */
+g2g_status g2g_plan_create_cast(const g2g_layout_desc *initial, g2g_dtype src_dtype,
+                                const g2g_layout_desc *final_, g2g_dtype dst_dtype,
+                                const g2g_op *op, void *stream, g2g_plan **plan);
+
+/* Plans, executes and destroys a cast transform; returns after completion. */
+g2g_status g2g_transform_cast(const g2g_layout_desc *initial, g2g_dtype src_dtype,
+                              const g2g_layout_desc *final_, g2g_dtype dst_dtype,
+                              const g2g_op *op, void *stream);
+
 /* ---- one-shot transform ------------------------------------------------ */
 
 /* plan + execute, returning after the transform completed: the reference's

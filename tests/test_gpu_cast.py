@@ -1,0 +1,106 @@
+"""Fused dtype cast (g2g_transform_cast): final = convert(op(initial)) on
+the GPU against numpy's conversions of the same matrices (the reference has
+no such operation). Bit-exact except NaN payloads, which IEEE leaves to the
+implementation (compared as NaN)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from grid2grid_gb300 import capi
+from grid2grid_gb300 import layouts as Ls
+
+import g2g_testlib as T
+
+NP = {capi.FLOAT32: np.float32, capi.FLOAT64: np.float64,
+      capi.COMPLEX64: np.complex64, capi.COMPLEX128: np.complex128}
+CASTS = [(capi.FLOAT64, capi.FLOAT32), (capi.FLOAT32, capi.FLOAT64),
+         (capi.COMPLEX128, capi.COMPLEX64), (capi.COMPLEX64, capi.COMPLEX128),
+         (capi.FLOAT32, capi.COMPLEX64), (capi.FLOAT64, capi.COMPLEX128),
+         (capi.FLOAT64, capi.COMPLEX64), (capi.FLOAT32, capi.COMPLEX128)]
+
+
+def _values(rng, L, dt):
+    """A source arena of finite values spanning many exponents plus special
+    values (inf, nan, subnormals, values that overflow or underflow a float)."""
+    a = np.zeros(L.arena_bytes, np.uint8)
+    base = np.float64 if dt in (capi.FLOAT64, capi.COMPLEX128) else np.float32
+    for b in range(L.n_blocks):
+        v = L.block_view(a, b)
+        n = v.size * (2 if dt in (capi.COMPLEX64, capi.COMPLEX128) else 1)
+        x = rng.standard_normal(n) * np.exp2(rng.integers(-140, 140, size=n))
+        special = np.array([np.inf, -np.inf, np.nan, 0.0, -0.0, 1e-45, 3.5e38, 1e300, -1e-310])
+        k = rng.integers(0, n, size=max(1, n // 50))
+        x[k] = rng.choice(special, size=len(k))
+        with np.errstate(over="ignore"):
+            xs = x.astype(base)
+        v[...] = xs.view(v.dtype).reshape(v.shape) if v.size else v
+    return a
+
+
+def _expected(Li, Lf, ai, af, src, dst, trans):
+    g = Li.gather(ai).view(NP[src])          # op(initial) in the final coordinates
+    with np.errstate(over="ignore", invalid="ignore"):
+        x = g.astype(NP[dst])
+    if trans == "C" and np.iscomplexobj(x):
+        x = np.conj(x)
+    out = af.copy()
+    for b in range(Lf.n_blocks):
+        i, j = int(Lf.blocks["row"][b]), int(Lf.blocks["col"][b])
+        blk = x[Lf.rows_split[i]:Lf.rows_split[i + 1], Lf.cols_split[j]:Lf.cols_split[j + 1]]
+        v = Lf.block_view(out, b)
+        v[...] = np.ascontiguousarray(blk).view(v.dtype).reshape(v.shape) if v.size else v
+    return out
+
+
+def _layouts(rng, src, dst, trans, m=257, n=190, P=5):
+    Li = Ls.random_grid_layout(m if trans == "N" else n, n if trans == "N" else m, P, src, rng,
+                               ext_hi=70)
+    Lf = Ls.random_grid_layout(m, n, P, dst, rng, ext_hi=70)
+    return Li, Lf
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("src,dst", CASTS)
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+def test_cast_matches_numpy(src, dst, trans):
+    import torch
+    rng = np.random.default_rng(100 * src + 10 * dst + "NTC".index(trans))
+    Li, Lf = _layouts(rng, src, dst, trans)
+    ai = _values(rng, Li, src)
+    af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
+    Lt = Li.copy().transpose_or_conjugate(trans) if trans != "N" else Li
+    want = _expected(Lt, Lf, ai, af, src, dst, trans)
+    lib = capi.load()
+    di, df = T.to_device([ai, af])
+    dI, k1 = Li.desc(di.data_ptr())
+    dF, k2 = Lf.desc(df.data_ptr())
+    op = capi.make_op(trans, 1.0, 0.0)
+    capi.check(lib.g2g_transform_cast(C.byref(dI), src, C.byref(dF), dst, C.byref(op), None))
+    torch.cuda.synchronize()
+    got = df.cpu().numpy()
+    comp = 8 if dst in (capi.FLOAT64, capi.COMPLEX128) else 4
+    Lcmp = Ls.Layout(Lf.rows_split, Lf.cols_split, Lf.owners, Lf.n_ranks,
+                     capi.FLOAT64 if comp == 8 else capi.FLOAT32, [], [], [], [], [], 0)
+    T.assert_arenas_equal(got, want, Lcmp, nan_equivalent=True,
+                          what=f"cast {src}->{dst} op {trans}")
+
+
+def test_cast_argument_checks():
+    """Complex -> real and scaled casts are refused on the host."""
+    lib = capi.load()
+    rng = np.random.default_rng(1)
+    Li, Lf = _layouts(rng, capi.COMPLEX64, capi.FLOAT32, "N", m=20, n=20)
+    dI, k1 = Li.desc(1 << 20)
+    dF, k2 = Lf.desc(1 << 30)
+    plan = C.c_void_p()
+    st = lib.g2g_plan_create_cast(C.byref(dI), capi.COMPLEX64, C.byref(dF), capi.FLOAT32,
+                                  None, None, C.byref(plan))
+    assert st == capi.ERROR_UNSUPPORTED
+    Li, Lf = _layouts(rng, capi.FLOAT64, capi.FLOAT32, "N", m=20, n=20)
+    dI, k1 = Li.desc(1 << 20)
+    dF, k2 = Lf.desc(1 << 30)
+    op = capi.make_op("N", 2.0, 0.0)
+    st = lib.g2g_plan_create_cast(C.byref(dI), capi.FLOAT64, C.byref(dF), capi.FLOAT32,
+                                  C.byref(op), None, C.byref(plan))
+    assert st == capi.ERROR_UNSUPPORTED
