@@ -85,11 +85,16 @@ size_t ring_smem_bytes(const ScatterConfig &cfg);
 // memory limit first when it is above the default. Computed once per
 // (device, kernel, threads, smem) and cached: launches pay a table lookup.
 cudaError_t kernel_occupancy(const void *fn, int threads, size_t smem, int *occ);
-// The kernel instances by CTA size (one translation unit each).
+// The kernel instances by CTA size, plain and element-arithmetic plans
+// apart (one translation unit each, compiled in parallel).
 cudaError_t launch_scatter_256(const PlanList &list, const ScatterConfig &cfg,
                                cudaStream_t stream);
 cudaError_t launch_scatter_512(const PlanList &list, const ScatterConfig &cfg,
                                cudaStream_t stream);
+cudaError_t launch_scatter_256_elem(const PlanList &list, const ScatterConfig &cfg,
+                                    cudaStream_t stream);
+cudaError_t launch_scatter_512_elem(const PlanList &list, const ScatterConfig &cfg,
+                                    cudaStream_t stream);
 
 
 // Shared memory a transposed tile of edge `tile_dim` with elements of `esz`

@@ -1,6 +1,8 @@
 // Host side of the gather-scatter: shared-memory sizes of the kernel variants
-// and the launch entry, which dispatches to the per-CTA-size translation
-// units (g2g_scatter_256.cu, g2g_scatter_512.cu) so they compile in parallel.
+// and the launch entry, which dispatches to the translation units of the
+// kernel instances (g2g_scatter_256.cu, g2g_scatter_512.cu and their
+// element-arithmetic counterparts g2g_scatter_256e.cu, g2g_scatter_512e.cu),
+// compiled in parallel.
 #include "g2g_scatter_impl.cuh"
 
 #include <map>
@@ -69,9 +71,14 @@ cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,
         return cudaErrorInvalidConfiguration;
     if (list.total_copy + list.total_cta <= 0)
         return cudaSuccess;
+    const bool elem = (cfg.paths & (PATH_SCALED | PATH_CAST)) != 0;
     switch (cfg.threads) {
-    case 512: return launch_scatter_512(list, cfg, stream);
-    default: return launch_scatter_256(list, cfg, stream);
+    case 512:
+        return elem ? launch_scatter_512_elem(list, cfg, stream)
+                    : launch_scatter_512(list, cfg, stream);
+    default:
+        return elem ? launch_scatter_256_elem(list, cfg, stream)
+                    : launch_scatter_256(list, cfg, stream);
     }
 }
 

@@ -1,11 +1,12 @@
-// Gather-scatter kernel instances with 512-thread CTAs.
+// Gather-scatter kernel instances with 512-thread CTAs: plain copies and
+// transposes.
 #include "g2g_scatter_impl.cuh"
 
 namespace g2g {
 
 cudaError_t launch_scatter_512(const PlanList &list, const ScatterConfig &cfg,
                                cudaStream_t stream) {
-    return launch_p<512>(list, cfg, stream);
+    return launch_plain_paths<512>(list, cfg, stream);
 }
 
 } // namespace g2g

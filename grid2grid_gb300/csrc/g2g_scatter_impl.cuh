@@ -1905,8 +1905,19 @@ cudaError_t launch_u(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s
     }
 }
 
+// Plans with plain copies and transposes only.
 template <int THREADS>
-cudaError_t launch_p(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
+cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
+    if (cfg.paths == PATH_COPY)
+        return launch_u<THREADS, PATH_COPY>(l, cfg, s);
+    if (cfg.paths == PATH_TRANSPOSE)
+        return launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
+    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
+}
+
+// Plans with element arithmetic: scaled or cast tiles (and any others).
+template <int THREADS>
+cudaError_t launch_elem_paths(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
     if (cfg.paths & PATH_CAST) {
         if (cfg.paths & PATH_SCALED) // not generated: cast and scaled plans launch apart
             return cudaErrorNotSupported;
@@ -1914,13 +1925,7 @@ cudaError_t launch_p(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s
     }
     if (cfg.paths & PATH_SCALED_COMPLEX)
         return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED>(l, cfg, s);
-    if (cfg.paths & PATH_SCALED_REAL)
-        return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED_REAL>(l, cfg, s);
-    if (cfg.paths == PATH_COPY)
-        return launch_u<THREADS, PATH_COPY>(l, cfg, s);
-    if (cfg.paths == PATH_TRANSPOSE)
-        return launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
-    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
+    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_SCALED_REAL>(l, cfg, s);
 }
 
 } // namespace
