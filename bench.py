@@ -406,7 +406,7 @@ def run_ours(args):
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
                      "tuning": {k: getattr(info.tuning, k) for k in
                                 ("tile_bytes", "tile_dim", "ctas_per_sm", "threads",
-                                 "unroll", "stages", "ring", "tile_run")}},
+                                 "unroll", "stages", "ring", "tile_run", "l2_prefetch")}},
         }
         print(json.dumps(line))
     if ws > 1:
@@ -540,7 +540,7 @@ def run_batched(lib, dev, stream, steps, peak):
                     "plan_ms": round(plan_ms, 1),
                     "tuning": {k: getattr(tuned, k) for k in
                                ("tile_bytes", "tile_dim", "ctas_per_sm", "threads", "unroll",
-                                "stages", "ring", "tile_run")},
+                                "stages", "ring", "tile_run", "l2_prefetch")},
                     "graph": True},
         "plain_launches": {"value": round(b / (ms_p * 1e-3) / 1e9, 2), "unit": UNIT,
                            "ms_per_step": round(ms_p, 4), "launches_per_step": n,

@@ -80,6 +80,7 @@ class Tuning(C.Structure):
         ("stages", C.c_int32),
         ("ring", C.c_int32),
         ("tile_run", C.c_int32),
+        ("l2_prefetch", C.c_int32),
     ]
 
 

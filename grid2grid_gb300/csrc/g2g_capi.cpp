@@ -296,6 +296,7 @@ g2g_tuning default_tuning() {
     t.stages = -1; // TMA staging is opt-in (no faster on measured workloads)
     t.ring = 1;
     t.tile_run = 1;
+    t.l2_prefetch = -1;
     return t;
 }
 
@@ -311,6 +312,7 @@ g2g_tuning merge_tuning(const g2g_tuning &base, const g2g_tuning *over) {
     if (over->stages) t.stages = over->stages;
     if (over->ring) t.ring = over->ring;
     if (over->tile_run) t.tile_run = over->tile_run;
+    if (over->l2_prefetch) t.l2_prefetch = over->l2_prefetch;
     return t;
 }
 
@@ -330,6 +332,8 @@ g2g_status check_tuning(const g2g_tuning &t) {
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ring must be -1 or 1");
     if (t.tile_run < 1 || t.tile_run > 64 || (t.tile_run & (t.tile_run - 1)))
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_run must be a power of two in [1, 64]");
+    if (t.l2_prefetch != -1 && t.l2_prefetch != 1)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: l2_prefetch must be -1 or 1");
     if (t.ctas_per_sm < 1 || t.ctas_per_sm > 32)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ctas_per_sm outside [1, 32]");
     return G2G_SUCCESS;
@@ -733,6 +737,7 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     c.run_shift = 0;
     while ((1 << c.run_shift) < pl.tuning.tile_run && c.run_shift < 6)
         ++c.run_shift;
+    c.l2_prefetch = pl.tuning.l2_prefetch == 1 ? 1 : 0;
     c.stages = 0;
     if ((c.paths & 1) && pl.tuning.stages >= 2 && !pl.host_memory) {
         c.stage_bytes = g2g::stage_bytes_for(pl.tuning.tile_bytes);
@@ -1136,6 +1141,7 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
     const int stage_opts[] = {-1, 2, 3, 4};
     const int ring_opts[] = {1, -1};
     const int run_opts[] = {1, 2};
+    const int prefetch_opts[] = {-1, 1};
     for (int tb : tile_bytes_opts)
         for (int td : tile_dim_opts) {
             if (!plan->any_trans && td != start.tile_dim)
@@ -1145,26 +1151,31 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
                     for (int c : ctas_opts)
                         for (int sg : stage_opts)
                             for (int rg : ring_opts)
-                                for (int run : run_opts) {
-                                    if (th * c > 2048)
-                                        continue;
-                                    if ((sg != -1 || rg != 1) && !(plan->paths & 1))
-                                        continue;
-                                    if (sg != -1 && rg != 1)
-                                        continue;
-                                    if (run != 1 && (sg != -1 || rg != 1))
-                                        continue; // runs only matter to the ring
-                                    g2g_tuning t = start;
-                                    t.tile_bytes = tb;
-                                    t.tile_dim = td;
-                                    t.threads = th;
-                                    t.unroll = u;
-                                    t.ctas_per_sm = c;
-                                    t.stages = sg;
-                                    t.ring = rg;
-                                    t.tile_run = run;
-                                    cands.push_back(t);
-                                }
+                                for (int run : run_opts)
+                                    for (int pf : prefetch_opts) {
+                                        if (th * c > 2048)
+                                            continue;
+                                        if ((sg != -1 || rg != 1) && !(plan->paths & 1))
+                                            continue;
+                                        if (sg != -1 && rg != 1)
+                                            continue;
+                                        // runs and prefetch only matter to the ring
+                                        if ((run != 1 || pf != -1) && (sg != -1 || rg != 1))
+                                            continue;
+                                        if (run != 1 && pf != -1)
+                                            continue;
+                                        g2g_tuning t = start;
+                                        t.tile_bytes = tb;
+                                        t.tile_dim = td;
+                                        t.threads = th;
+                                        t.unroll = u;
+                                        t.ctas_per_sm = c;
+                                        t.stages = sg;
+                                        t.ring = rg;
+                                        t.tile_run = run;
+                                        t.l2_prefetch = pf;
+                                        cands.push_back(t);
+                                    }
         }
     cudaEvent_t e0, e1;
     G2G_CUDA(cudaEventCreate(&e0));

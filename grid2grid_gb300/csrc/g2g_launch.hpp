@@ -69,8 +69,11 @@ struct ScatterConfig {
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
     int ring = 0;            // plain copies through the per-warp cp.async ring
     int run_shift = 0;       // ring: runs of 2^run_shift consecutive tiles per warp
+    int l2_prefetch = 0;     // ring: bulk L2 prefetch of each tile's source columns
     int stage_bytes = 0;     // bytes per stage
     size_t trans_bytes = 0;  // shared memory for direct transposed / scaled tiles
+    bool dry_run = false;    // prepare the kernel instance (load it, query its
+                             // occupancy, raise its shared-memory limit), no launch
 };
 
 // Stage size that holds any plain tile of `tile_bytes` whose columns are at
@@ -104,5 +107,10 @@ size_t transpose_smem_bytes(int tile_dim, int esz);
 // Launches the gather-scatter over the plans of `list`.
 cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,
                            cudaStream_t stream);
+
+// Prepares every kernel instance a plan or a merged launch can select on the
+// current device (dry runs of launch_scatter), so that no later launch pays
+// for loading its module lazily.
+cudaError_t preload_scatter_kernels();
 
 } // namespace g2g

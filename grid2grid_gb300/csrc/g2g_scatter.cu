@@ -82,4 +82,35 @@ cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,
     }
 }
 
+cudaError_t preload_scatter_kernels() {
+    PlanList list;
+    list.n = 1;
+    list.total_copy = 1;
+    const int path_sets[] = {PATH_COPY, PATH_TRANSPOSE, PATH_COPY | PATH_TRANSPOSE,
+                             PATH_COPY | PATH_SCALED_REAL, PATH_COPY | PATH_SCALED_COMPLEX,
+                             PATH_COPY | PATH_CAST};
+    for (int threads : {256, 512})
+        for (int unroll : {1, 2, 4})
+            for (int paths : path_sets)
+                for (int mode = 0; mode <= 4; ++mode) { // direct, ring, 2..4 stages
+                    if (mode >= 1 && !(paths & PATH_COPY))
+                        continue;
+                    ScatterConfig c;
+                    c.threads = threads;
+                    c.unroll = unroll;
+                    c.grid = 1;
+                    c.paths = paths;
+                    c.tile_dim = 32;
+                    c.trans_bytes = c.smem_bytes = transpose_smem_bytes(32, 16);
+                    c.ring = mode == 1;
+                    c.stages = mode >= 2 ? mode : 0;
+                    c.stage_bytes = stage_bytes_for(16 * 1024);
+                    c.dry_run = true;
+                    const cudaError_t e = launch_scatter(list, c, nullptr);
+                    if (e != cudaSuccess)
+                        return e;
+                }
+    return cudaSuccess;
+}
+
 } // namespace g2g

@@ -1462,6 +1462,9 @@ constexpr int RING_D = G2G_RING_D; // stages per warp ring (RING_D - 1 in flight
 constexpr int RING_LA = RING_D;
 constexpr int RING_Q = (2 * RING_D + 1 <= 8) ? 8 : 16; // entries; > RING_LA + RING_D
 constexpr int RING_QE = 64;                            // bytes per entry (a 48-byte Tile)
+// The ring kernel's option word: log2 of the run length, prefetch switch.
+constexpr int RING_OPT_RUN_MASK = 0xff;
+constexpr int RING_OPT_L2_PREFETCH = 0x100;
 static_assert(sizeof(Tile) <= RING_QE, "a Tile fits a queue entry");
 
 // Per-warp shared memory: RING_D stages of 32U + 1 blocks, the descriptor
@@ -1628,9 +1631,28 @@ struct RingOrder {
     long long base;   // first tile of the warp's first run
     long long stride; // tiles between the starts of its runs
     int shift;        // log2 of the run length
+    int l2_prefetch;  // bulk L2 prefetch of each multi-stage tile's columns
 };
 __device__ __forceinline__ long long tile_of(const RingOrder &o, int j) {
     return o.base + (long long)(j >> o.shift) * o.stride + (j & ((1 << o.shift) - 1));
+}
+
+// When a warp enters a tile of several stages and the plan asks for it,
+// each lane asks L2 for one source column of the tile in a single bulk
+// prefetch (a hint: nothing waits on it), so the tile's later stages find
+// their blocks in L2. Only the aligned 16-byte cover of each column is named,
+// which lies in the column's own blocks. It pays on plans of small tiles and
+// costs a little on 16 KB tiles of long columns, so it is a tuning switch.
+template <int U>
+__device__ __forceinline__ void ring_prefetch_tile(const RingTile &c, const RingOrder &o,
+                                                   int lane) {
+    if (!o.l2_prefetch || c.total <= 32 * U || c.L < 256 || lane >= c.cols)
+        return;
+    const uint64_t s = c.src + (uint64_t)((long long)lane * c.sld);
+    const uint64_t start = s & ~15ull, end = (s + (uint64_t)c.L + 15u) & ~15ull;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(start),
+                 "r"((uint32_t)(end - start))
+                 : "memory");
 }
 
 // The issuing side: its tile (index ti, ordinal j among the warp's tiles),
@@ -1662,6 +1684,7 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
                 ring_tile_init(q.c, *reinterpret_cast<const Tile *>(
                                         queue + (q.j & (RING_Q - 1)) * RING_QE));
                 ring_walk_init(q.w, q.c, lane);
+                ring_prefetch_tile<U>(q.c, ord, lane);
                 ring_queue_fetch(list, tile_of(ord, q.j + RING_LA),
                                  queue_s + (uint32_t)(((q.j + RING_LA) & (RING_Q - 1)) * RING_QE),
                                  lane);
@@ -1680,7 +1703,7 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
 
 template <int U>
 __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
-                                                int warp, int nwarp, int run_shift) {
+                                                int warp, int nwarp, int ring_opts) {
     constexpr int SLOT_BYTES = ring_stage_bytes<U>();
     const int lane = threadIdx.x & 31;
     unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
@@ -1690,7 +1713,9 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     const uint32_t queue_s = smem_addr(queue);
     const long long GW = (long long)gridDim.x * nwarp;
     RingOrder ord;
+    const int run_shift = ring_opts & RING_OPT_RUN_MASK;
     ord.shift = run_shift;
+    ord.l2_prefetch = ring_opts & RING_OPT_L2_PREFETCH;
     ord.base = ((long long)blockIdx.x * nwarp + warp) << run_shift;
     ord.stride = GW << run_shift;
     RingIssue q;
@@ -1714,6 +1739,7 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     if (q.ti < list.total_copy) {
         ring_tile_init(q.c, *reinterpret_cast<const Tile *>(queue));
         ring_walk_init(q.w, q.c, lane);
+        ring_prefetch_tile<U>(q.c, ord, lane);
     }
 #pragma unroll
     for (int st = 0; st < RING_D - 1; ++st)
@@ -1759,10 +1785,10 @@ template <int THREADS, int PATHS> struct RingMinBlocks {
 
 template <int THREADS, int U, int PATHS>
 __global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS, PATHS>::value))
-    scatter_ring_kernel(const __grid_constant__ PlanList list, int td, int run_shift) {
+    scatter_ring_kernel(const __grid_constant__ PlanList list, int td, int ring_opts) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;
-    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP, run_shift);
+    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP, ring_opts);
     if (PATHS & (PATH_TRANSPOSE | PATH_SCALED | PATH_CAST)) {
         __syncthreads(); // the ring's shared memory becomes the CTA tiles'
         cta_phase<THREADS, PATHS>(list, smem, td);
@@ -1856,7 +1882,7 @@ cudaError_t launch_staged(const PlanList &list, const ScatterConfig &cfg, cudaSt
     const size_t smem = staged_smem_bytes(cfg);
     unsigned grid = 0;
     cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess || cfg.dry_run)
         return e;
     k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim, cfg.stage_bytes);
     return cudaGetLastError();
@@ -1868,9 +1894,10 @@ cudaError_t launch_ring(const PlanList &list, const ScatterConfig &cfg, cudaStre
     const size_t smem = ring_smem_bytes(cfg);
     unsigned grid = 0;
     cudaError_t e = prepare(k, cfg, smem, list.total_copy + list.total_cta, grid);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess || cfg.dry_run)
         return e;
-    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim, cfg.run_shift);
+    k<<<grid, THREADS, smem, s>>>(list, cfg.tile_dim,
+                                  cfg.run_shift | (cfg.l2_prefetch ? RING_OPT_L2_PREFETCH : 0));
     return cudaGetLastError();
 }
 
@@ -1890,7 +1917,7 @@ cudaError_t launch_t(const PlanList &list, const ScatterConfig &cfg, cudaStream_
     auto k = scatter_kernel<THREADS, U, PATHS>;
     unsigned grid = 0;
     cudaError_t e = prepare(k, cfg, cfg.smem_bytes, list.total_copy + list.total_cta, grid);
-    if (e != cudaSuccess)
+    if (e != cudaSuccess || cfg.dry_run)
         return e;
     k<<<grid, THREADS, cfg.smem_bytes, s>>>(list, cfg.tile_dim);
     return cudaGetLastError();

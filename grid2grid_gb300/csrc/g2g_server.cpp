@@ -302,6 +302,10 @@ g2g_status g2g_server_create(const g2g_server_config *config, g2g_server **out) 
     if (s->cfg.plan_cache_entries <= 0)
         s->cfg.plan_cache_entries = 4096;
     cudaError_t e = cudaGetDevice(&s->device);
+    // every kernel instance a batch can select is loaded now, not by the
+    // first request that needs it (a lazily loaded module costs milliseconds)
+    if (e == cudaSuccess)
+        e = g2g::preload_scatter_kernels();
     for (int k = 0; e == cudaSuccess && k < s->cfg.max_launches_in_flight; ++k) {
         cudaStream_t st;
         e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);

@@ -139,6 +139,9 @@ typedef struct g2g_tuning {
                                  through registers (0 = default)            */
     int32_t tile_run;         /* ring: a warp takes runs of this many
                                  consecutive tiles (1, 2, 4 .. 64; 0 = default) */
+    int32_t l2_prefetch;      /* ring: 1 = a warp entering a tile asks L2 for
+                                 the tile's source columns in bulk, -1 = no
+                                 (0 = default: no)                          */
 } g2g_tuning;
 
 typedef struct g2g_plan_info {
@@ -388,6 +391,9 @@ typedef struct g2g_server_stats {
     int64_t inflight_bytes_peak;
 } g2g_server_stats;
 
+/* Creates the server on the current device and loads every gather-scatter
+ * kernel instance a launch can select there, so that no request waits for a
+ * lazily loaded module. */
 g2g_status g2g_server_create(const g2g_server_config *config, g2g_server **server);
 
 /* Queues a transform; *ticket identifies it. Fails with G2G_ERROR_BUDGET if

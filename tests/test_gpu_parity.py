@@ -170,7 +170,8 @@ def test_mixed_dtype_batch_matches_port():
     dict(threads=256, unroll=1, ring=-1), dict(threads=512, unroll=4, ring=-1),
     dict(threads=256, unroll=2, ring=1), dict(threads=512, unroll=1, ring=1),
     dict(tile_bytes=512, unroll=4, ring=1, ctas_per_sm=1),
-    dict(tile_bytes=2048, ring=1, tile_run=8), dict(threads=256, ring=1, tile_run=64)])
+    dict(tile_bytes=2048, ring=1, tile_run=8), dict(threads=256, ring=1, tile_run=64),
+    dict(tile_bytes=4096, ring=1, l2_prefetch=1), dict(threads=256, unroll=1, ring=1, l2_prefetch=1)])
 def test_tunings_give_identical_results(tuning):
     rng = np.random.default_rng(77)
     inits, finals, ias, fas, ops = [], [], [], [], []
