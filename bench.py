@@ -257,6 +257,8 @@ def _config(w, args):
     c["l2"] = "inputs larger than L2 (no flush)" if w.bytes_moved >= 512 * 2**20 else \
         "L2 flushed between steps (512 MiB write, then 256 MiB read of another buffer)"
     c["parallelism"] = f"replicas x{args.gpus}"
+    if getattr(args, "alpha_beta", None) is not None:
+        c["alpha_beta"] = list(args.alpha_beta)
     return c
 
 
@@ -294,7 +296,11 @@ def run_ours(args):
     dI, dF = descs(w.inits, dev_i), descs(w.finals, dev_f)
     dts = (C.c_int * n)(*w.dtypes())
     ops = None
-    if w.ops is not None:
+    if args.alpha_beta is not None: # the workload's op letters, scaled
+        a, b = args.alpha_beta
+        ops = (capi.Op * n)(*[capi.make_op(w.ops[k][0] if w.ops else "N", a, b)
+                              for k in range(n)])
+    elif w.ops is not None:
         ops = (capi.Op * n)(*[capi.make_op(*o) for o in w.ops])
     stream = torch.cuda.Stream(device=dev)
     sp = C.c_void_p(stream.cuda_stream)
@@ -307,7 +313,8 @@ def run_ours(args):
         t = capi.Tuning()
         capi.check(lib.g2g_plan_autotune(plan, sp, 3, C.byref(t)))
         tuned = {k: getattr(t, k) for k in ("tile_bytes", "tile_dim", "ctas_per_sm",
-                                            "threads", "unroll")}
+                                            "threads", "unroll", "stages", "ring",
+                                            "tile_run", "l2_prefetch")}
     info = capi.PlanInfo()
     capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
     # warm-up
@@ -361,7 +368,8 @@ def run_ours(args):
     value = replica_value(bytes_step, ms_per_step, ws)
     peak, peak_kind = _peaks()
     achieved = info.bytes_min_traffic / (kernel_ms * 1e-3) / 1e9
-    traffic = _profile_traffic("g2g_scatter", w.name)
+    # the scaled kernel's capture is its own summary (profiles/*_scaled.md)
+    traffic = _profile_traffic("g2g_scatter", w.name + ("_scaled" if args.alpha_beta else ""))
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "peak_source": peak_kind,
@@ -758,6 +766,10 @@ def main(argv=None):
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-reps", type=int, default=2)
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--alpha-beta", type=lambda v: tuple(float(x) for x in v.split(",")),
+                    default=None, metavar="A,B",
+                    help="time final = B*final + A*op(initial) on the workload instead "
+                         "of its plain transform (the scaled kernel instances)")
     ap.add_argument("--no-batch", dest="batch", action="store_false",
                     help="skip the 256-transform batched stream")
     ap.add_argument("--no-serving", dest="serving", action="store_false",

@@ -120,10 +120,14 @@ __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
     }
 }
 
-// Plain copies are warp-level work items, transposed and scaled tiles
-// CTA-level ones; the work list holds all copy tiles first.
+// Plain copies and non-transposed scaled tiles whose destination elements
+// never straddle a 16-byte chunk are warp-level work items, the other
+// transposed, scaled and converting tiles CTA-level ones; the work list holds
+// all warp-level tiles first.
 __device__ inline bool is_copy_kind(uint32_t kind) {
-    return !(kind & (KIND_TRANS | KIND_SCALED | KIND_CAST));
+    if (kind & (KIND_TRANS | KIND_CAST))
+        return false;
+    return !(kind & KIND_SCALED) || (kind & KIND_WARP_SCALED);
 }
 
 __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pairs,

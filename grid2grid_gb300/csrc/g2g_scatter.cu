@@ -55,9 +55,14 @@ int stage_bytes_for(int tile_bytes) {
 
 size_t ring_smem_bytes(const ScatterConfig &cfg) {
     const int u = cfg.unroll == 1 ? 1 : (cfg.unroll == 2 ? 2 : 4);
-    const size_t ring = (size_t)(cfg.threads / 32) *
-                        (size_t)(u == 1 ? ring_warp_bytes<1>()
-                                        : (u == 2 ? ring_warp_bytes<2>() : ring_warp_bytes<4>()));
+    // kernels with scaled tiles stage destination chunks as well
+    const size_t per_warp =
+        (cfg.paths & PATH_SCALED)
+            ? (size_t)(u == 1 ? ring_warp_bytes<1, true>()
+                              : (u == 2 ? ring_warp_bytes<2, true>() : ring_warp_bytes<4, true>()))
+            : (size_t)(u == 1 ? ring_warp_bytes<1, false>()
+                              : (u == 2 ? ring_warp_bytes<2, false>() : ring_warp_bytes<4, false>()));
+    const size_t ring = (size_t)(cfg.threads / 32) * per_warp;
     return ring > cfg.trans_bytes ? ring : cfg.trans_bytes;
 }
 

@@ -1406,6 +1406,40 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     }
 }
 
+// A warp-level work item on the register path: a plain copy, or (kernels
+// with scaled tiles) a non-transposed scaled tile, by NWARP warps.
+template <int NWARP, int U, int PATHS>
+__device__ __forceinline__ void warp_tile(const Tile &t, int warp, const PairInfo *pairs) {
+    if constexpr ((PATHS & PATH_SCALED) != 0) {
+        if (t.kind & KIND_SCALED) {
+            switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
+            case 0:
+                if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+                    scaled_copy_tile<NWARP, 2, float>(t, warp, scalar_from<float>(pairs[t.pair].alpha),
+                                                      scalar_from<float>(pairs[t.pair].beta));
+                break;
+            case 1:
+                if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+                    scaled_copy_tile<NWARP, 2, double>(t, warp, scalar_from<double>(pairs[t.pair].alpha),
+                                                       scalar_from<double>(pairs[t.pair].beta));
+                break;
+            case 2:
+                if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+                    scaled_copy_tile<NWARP, 2, cplxf>(t, warp, scalar_from<cplxf>(pairs[t.pair].alpha),
+                                                      scalar_from<cplxf>(pairs[t.pair].beta));
+                break;
+            default:
+                if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+                    scaled_copy_tile<NWARP, 2, cplxd>(t, warp, scalar_from<cplxd>(pairs[t.pair].alpha),
+                                                      scalar_from<cplxd>(pairs[t.pair].beta));
+                break;
+            }
+            return;
+        }
+    }
+    copy_tile<NWARP, U>(t, warp);
+}
+
 template <int THREADS, int U, int PATHS>
 __global__ void __launch_bounds__(THREADS, (MinBlocksP<PATHS, U, THREADS>::value))
     scatter_kernel(const __grid_constant__ PlanList list, int td) {
@@ -1424,7 +1458,7 @@ __global__ void __launch_bounds__(THREADS, (MinBlocksP<PATHS, U, THREADS>::value
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(locate_copy(list, ti + GW, unused)));
             }
             const Tile t = *locate_copy(list, ti, pairs);
-            copy_tile<1, U>(t, 0);
+            warp_tile<1, U, PATHS>(t, 0, pairs);
         }
     }
     // phase 2: transposed and scaled tiles, one CTA per tile
@@ -1467,13 +1501,16 @@ constexpr int RING_OPT_RUN_MASK = 0xff;
 constexpr int RING_OPT_L2_PREFETCH = 0x100;
 static_assert(sizeof(Tile) <= RING_QE, "a Tile fits a queue entry");
 
-// Per-warp shared memory: RING_D stages of 32U + 1 blocks, the descriptor
-// queue, one valid flag per stage (0: no stage, the warp's work is done).
-template <int U> __host__ __device__ constexpr int ring_stage_bytes() {
-    return (U * 32 + 1) * 16;
+// Per-warp shared memory: RING_D stages of 32U + 1 source blocks (and, in
+// kernels with scaled tiles, the 32U destination chunks they update), the
+// descriptor queue, one valid flag per stage (0: no stage, the warp's work is
+// done).
+template <int U, bool SC> __host__ __device__ constexpr int ring_stage_bytes() {
+    return (U * 32 + 1) * 16 + (SC ? U * 32 * 16 : 0);
 }
-template <int U> __host__ __device__ constexpr int ring_warp_bytes() {
-    return RING_D * ring_stage_bytes<U>() + RING_Q * RING_QE + ((RING_D * 4 + 15) / 16) * 16;
+template <int U, bool SC> __host__ __device__ constexpr int ring_warp_bytes() {
+    return RING_D * ring_stage_bytes<U, SC>() + RING_Q * RING_QE +
+           ((RING_D * 4 + 15) / 16) * 16;
 }
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
@@ -1504,8 +1541,12 @@ struct RingTile {
     int cols, L, cpc, dq, dr, total;
     float rcp; // 1 / cpc, for the quotients of small numbers by cpc
     bool aligned;
+    uint32_t kind; // KIND_SCALED: beta*dst + alpha*src (dtype in the kind)
+    int pair;
 };
 __device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
+    c.kind = t.kind;
+    c.pair = t.pair;
     c.dst = t.dst;
     c.src = t.src;
     c.dld = t.dst_ld;
@@ -1554,10 +1595,14 @@ __device__ __forceinline__ void ring_walk_step(RingWalk &w, const RingTile &c) {
     }
 }
 
-// Issues the cp.async copies of one stage into ring slots `slots`.
-template <int U>
+// Issues the cp.async copies of one stage into ring slots `slots`; for a
+// scaled tile (SC kernels) also the destination chunks, after the source
+// blocks. Only this lane's own destination words of a chunk are ever stored,
+// and no other work item writes them, so the chunk's other words may be stale.
+template <int U, bool SC>
 __device__ __forceinline__ void ring_issue(const RingTile &c, RingWalk &w, uint32_t slots,
                                            int lane) {
+    const bool scaled = SC && (c.kind & KIND_SCALED);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         if (w.col < c.cols) {
@@ -1572,6 +1617,9 @@ __device__ __forceinline__ void ring_issue(const RingTile &c, RingWalk &w, uint3
                 cp_async16(slot, base + (uint64_t)rel);
             if (u == U - 1 && lane == 31 && sh != 0 && rel + 16 < hi)
                 cp_async16(slot + 16, base + (uint64_t)(rel + 16));
+            if (scaled && rel + 16 > d0 && rel < d0 + c.L)
+                cp_async16(slot + (uint32_t)((U * 32 + 1) * 16),
+                           w.d - (uint64_t)d0 + (uint64_t)rel);
         }
         ring_walk_step(w, c);
     }
@@ -1609,6 +1657,70 @@ __device__ __forceinline__ void ring_store(const RingTile &c, RingWalk &w, uint3
             }
         }
         ring_walk_step(w, c);
+    }
+}
+
+// Stores one landed stage of a scaled tile: each destination chunk becomes
+// beta*d + alpha*s on its whole elements (the pair's alpha and beta, rounded
+// as scaled_copy_tile rounds them), then the chunk walk's word-masked store.
+template <int U, typename T>
+__device__ __forceinline__ void ring_store_scaled(const RingTile &c, RingWalk &w,
+                                                  uint32_t slots, int lane,
+                                                  const PairInfo *pp) {
+    const T alpha = scalar_from<T>(pp->alpha);
+    const T beta = scalar_from<T>(pp->beta);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        if (w.col < c.cols) {
+            const int d0 = (int)(w.d & 15u);
+            const int rel = w.k << 4;
+            const int end = d0 + c.L;
+            if (rel + 16 > d0 && rel < end) {
+                const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+                uint4 o = lds_ring(slot);
+                if (!c.aligned) {
+                    const int sh = (int)((w.s - (uint64_t)d0) & 15u);
+                    if (sh)
+                        o = funnel_words(o, lds_ring(slot + 16), (uint32_t)(sh >> 2));
+                }
+                o = axpby_chunk<T>(alpha, o, beta, lds_ring(slot + (uint32_t)((U * 32 + 1) * 16)));
+                const uint64_t chunk = w.d - (uint64_t)d0 + (uint64_t)rel;
+                if (rel >= d0 && rel + 16 <= end) {
+                    st_v4(chunk, o);
+                } else {
+                    const int wlo = rel >= d0 ? 0 : (d0 - rel) >> 2;
+                    const int whi = rel + 16 <= end ? 4 : (end - rel) >> 2;
+                    if (wlo <= 0 && whi > 0) st_u32(chunk, o.x);
+                    if (wlo <= 1 && whi > 1) st_u32(chunk + 4, o.y);
+                    if (wlo <= 2 && whi > 2) st_u32(chunk + 8, o.z);
+                    if (wlo <= 3 && whi > 3) st_u32(chunk + 12, o.w);
+                }
+            }
+        }
+        ring_walk_step(w, c);
+    }
+}
+template <int U, int PATHS>
+__device__ __forceinline__ void ring_store_scaled_dispatch(const RingTile &c, RingWalk &w,
+                                                           uint32_t slots, int lane,
+                                                           const PairInfo *pp) {
+    switch ((c.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0:
+        if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+            ring_store_scaled<U, float>(c, w, slots, lane, pp);
+        break;
+    case 1:
+        if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
+            ring_store_scaled<U, double>(c, w, slots, lane, pp);
+        break;
+    case 2:
+        if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+            ring_store_scaled<U, cplxf>(c, w, slots, lane, pp);
+        break;
+    default:
+        if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
+            ring_store_scaled<U, cplxd>(c, w, slots, lane, pp);
+        break;
     }
 }
 
@@ -1666,7 +1778,7 @@ struct RingIssue {
 };
 
 // Fills ring stage `st` from the issuing cursor (or marks it empty) and commits it.
-template <int U>
+template <int U, bool SC>
 __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
                                           const RingOrder &ord, uint32_t slots,
                                           const unsigned char *queue, uint32_t queue_s,
@@ -1674,7 +1786,7 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
     if (q.ti < list.total_copy) {
         if (lane == 0)
             *valid = 1;
-        ring_issue<U>(q.c, q.w, slots, lane);
+        ring_issue<U, SC>(q.c, q.w, slots, lane);
         q.idx0 += 32 * U;
         if (q.idx0 >= q.c.total) { // on to the warp's next tile
             ++q.j;
@@ -1701,12 +1813,13 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
     cp_async_commit();
 }
 
-template <int U>
+template <int U, int PATHS>
 __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
                                                 int warp, int nwarp, int ring_opts) {
-    constexpr int SLOT_BYTES = ring_stage_bytes<U>();
+    constexpr bool SC = (PATHS & PATH_SCALED) != 0;
+    constexpr int SLOT_BYTES = ring_stage_bytes<U, SC>();
     const int lane = threadIdx.x & 31;
-    unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U>();
+    unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U, SC>();
     unsigned char *queue = wbase + RING_D * SLOT_BYTES;
     int *valid = reinterpret_cast<int *>(queue + RING_Q * RING_QE);
     const uint32_t slots0 = smem_addr(wbase);
@@ -1743,19 +1856,20 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     }
 #pragma unroll
     for (int st = 0; st < RING_D - 1; ++st)
-        ring_fill<U>(list, q, ord, slots0 + (uint32_t)(st * SLOT_BYTES), queue, queue_s,
-                     valid + st, lane);
+        ring_fill<U, SC>(list, q, ord, slots0 + (uint32_t)(st * SLOT_BYTES), queue, queue_s,
+                         valid + st, lane);
     // the storing side: its tile ordinal, walk constants and position
     int js = -1;
     RingTile c;
     RingWalk w;
     int idx0 = 0;
     c.total = 0;
+    const PairInfo *pp = nullptr; // the scaled tile's pair (SC kernels)
     int sp = 0; // stage to store; the stage before it is filled next
     for (;;) {
         const int sf = sp == 0 ? RING_D - 1 : sp - 1;
-        ring_fill<U>(list, q, ord, slots0 + (uint32_t)(sf * SLOT_BYTES), queue, queue_s,
-                     valid + sf, lane);
+        ring_fill<U, SC>(list, q, ord, slots0 + (uint32_t)(sf * SLOT_BYTES), queue, queue_s,
+                         valid + sf, lane);
         cp_async_wait<RING_D - 1>();
         __syncwarp();
         if (!valid[sp]) // stages are filled in order: nothing after this
@@ -1766,8 +1880,17 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
                                   queue + (js & (RING_Q - 1)) * RING_QE));
             ring_walk_init(w, c, lane);
             idx0 = 0;
+            if (SC && (c.kind & KIND_SCALED)) {
+                const PairInfo *pairs;
+                locate_copy(list, tile_of(ord, js), pairs);
+                pp = pairs + c.pair;
+            }
         }
-        ring_store<U>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES), lane);
+        if (SC && (c.kind & KIND_SCALED))
+            ring_store_scaled_dispatch<U, PATHS>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES),
+                                                 lane, pp);
+        else
+            ring_store<U>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES), lane);
         idx0 += 32 * U;
         __syncwarp();
         sp = sp + 1 == RING_D ? 0 : sp + 1;
@@ -1788,7 +1911,7 @@ __global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS, PATHS>::value
     scatter_ring_kernel(const __grid_constant__ PlanList list, int td, int ring_opts) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int NWARP = THREADS / 32;
-    ring_copy_phase<U>(list, smem, threadIdx.x >> 5, NWARP, ring_opts);
+    ring_copy_phase<U, PATHS>(list, smem, threadIdx.x >> 5, NWARP, ring_opts);
     if (PATHS & (PATH_TRANSPOSE | PATH_SCALED | PATH_CAST)) {
         __syncthreads(); // the ring's shared memory becomes the CTA tiles'
         cta_phase<THREADS, PATHS>(list, smem, td);
@@ -1845,7 +1968,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             phase ^= 1u << st;
             consume_stage<THREADS, U>(t, stage);
         } else {
-            copy_tile<THREADS / 32, U>(t, warp);
+            warp_tile<THREADS / 32, U, PATHS>(t, warp, pairs);
         }
         __syncthreads(); // the stage is free again
         if (warp == 0)

@@ -317,11 +317,12 @@ def random_splits(total: int, rng: np.random.Generator, lo: int = 1, hi: int = 2
 
 def random_grid_layout(m, n, P, dtype, rng: np.random.Generator, *,
                        ext_lo=1, ext_hi=2048, pad_max=7, row_align=16,
-                       base_misalign=0, align=ALIGN) -> Layout:
+                       base_misalign=0, byte_misalign=0, align=ALIGN) -> Layout:
     """An arbitrary grid-like layout: seeded splits (extents U[ext_lo,
     ext_hi]), owners U[0, P) per block, each block its own allocation with
     stride = rows rounded up to ``row_align`` plus U[0, pad_max], placed at an
-    ``align``-byte aligned arena offset (+ ``base_misalign`` elements)."""
+    ``align``-byte aligned arena offset (+ ``base_misalign`` elements
+    + ``byte_misalign`` bytes)."""
     esz = capi.DTYPE_SIZE[dtype]
     rs = random_splits(m, rng, ext_lo, ext_hi)
     cs = random_splits(n, rng, ext_lo, ext_hi)
@@ -336,9 +337,10 @@ def random_grid_layout(m, n, P, dtype, rng: np.random.Generator, *,
             stride = (h + row_align - 1) // row_align * row_align + int(
                 rng.integers(0, pad_max + 1))
             ranks.append(int(owners[i, j])); rows.append(i); cols.append(j)
-            offs.append(off + base_misalign * esz)
+            lead = base_misalign * esz + byte_misalign
+            offs.append(off + lead)
             strides.append(stride)
-            off = _align(off + base_misalign * esz + stride * w * esz, align)
+            off = _align(off + lead + stride * w * esz, align)
     return Layout(rs, cs, owners, P, dtype, ranks, rows, cols, offs, strides,
                   max(off, align))
 

@@ -129,6 +129,48 @@ def test_scaled_match_port(dt, t):
         T.assert_arenas_equal(got, want, Lf, what=f"scaled dt{dt} {t} {alpha} {beta}")
 
 
+def _normal_arena(rng, L, dt):
+    comp = np.float32 if dt in (capi.FLOAT32, capi.COMPLEX64) else np.float64
+    n = L.arena_bytes // np.dtype(comp).itemsize
+    a = np.zeros(L.arena_bytes, np.uint8)
+    a[:n * np.dtype(comp).itemsize] = np.frombuffer(
+        rng.standard_normal(n).astype(comp).tobytes(), np.uint8)
+    return a
+
+
+@pytest.mark.parametrize("tuning", [
+    None, dict(ring=-1), dict(stages=2), dict(threads=512, unroll=2),
+    dict(tile_bytes=2048, unroll=1, l2_prefetch=1), dict(ring=1, tile_run=4)])
+def test_scaled_tiles_mixed_with_copies_match_port(tuning):
+    """Scaled pairs in one plan with plain and transposed ones. Non-transposed
+    scaled tiles are warp-level work items (on the copy ring, the register
+    path or beside the TMA-staged copies) when every destination element
+    lies in one 16-byte chunk; complex<float> blocks at 4 mod 8 and
+    complex<double> blocks at 8 mod 16 keep them CTA-level."""
+    rng = np.random.default_rng(303)
+    cases = [  # dtype, op, alpha, beta, destination byte misalignment
+        (capi.FLOAT32, "N", 2.0, 0.5, 4), (capi.FLOAT64, "N", -1.5, 0.25, 8),
+        (capi.COMPLEX64, "N", 0.5 + 1j, 0.25 - 0.5j, 0),
+        (capi.COMPLEX64, "N", 0.5 + 1j, 1.0 - 0.5j, 4),
+        (capi.COMPLEX128, "N", 2.0 - 1j, 0.5 + 0.5j, 0),
+        (capi.COMPLEX128, "N", 2.0 - 1j, 0.5 + 0.5j, 8),
+        (capi.FLOAT32, "T", 2.0, 0.5, 0), (capi.COMPLEX128, "C", 0.5, 2.0, 0),
+        (capi.FLOAT32, "N", 1.0, 0.0, 0), (capi.FLOAT64, "T", 1.0, 0.0, 0)]
+    inits, finals, ias, fas, ops = [], [], [], [], []
+    for dt, t, alpha, beta, mis in cases:
+        m, n = int(rng.integers(100, 400)), int(rng.integers(100, 400))
+        Li = Ls.random_grid_layout(m if t == "N" else n, n if t == "N" else m, 5, dt, rng,
+                                   ext_hi=150)
+        Lf = Ls.random_grid_layout(m, n, 5, dt, rng, ext_hi=150, byte_misalign=mis)
+        inits.append(Li); finals.append(Lf)
+        ias.append(_normal_arena(rng, Li, dt)); fas.append(_normal_arena(rng, Lf, dt))
+        ops.append((t, alpha, beta))
+    want = T.port_run(inits, finals, ias, fas, ops)
+    got = T.gpu_run(inits, finals, ias, fas, ops, how="plan", tuning=tuning)
+    for k in range(len(inits)):
+        T.assert_arenas_equal(got[k], want[k], finals[k], what=f"{tuning} case {cases[k]}")
+
+
 def test_scaled_special_values_nan_equivalent():
     """Inf/NaN through alpha/beta (Annex G complex products): equal up to NaN
     payloads, which IEEE leaves to the implementation."""
