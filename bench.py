@@ -704,7 +704,9 @@ def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
             capi.check(lib.g2g_plan_execute(plans[k % 2], C.c_void_p(st.cuda_stream)))
             for d, h in zip(sset["df"], sset["hf"]):
                 h.copy_(d, non_blocking=True)
-    for k in range(2):
+    # warm-up: a full trial's worth of steps (the first passes over the pinned
+    # arenas run measurably slower on the host link)
+    for k in range(max(2, steps)):
         pipe_step(k)
     torch.cuda.synchronize()
     trials = []
@@ -719,13 +721,32 @@ def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
     for p in plans:
         capi.check(lib.g2g_plan_destroy(p))
 
+    # the host-link bound of the same step: its copies alone, same streams
+    def copy_step(k):
+        sset = sets[k % 2]
+        with torch.cuda.stream(sset["stream"]):
+            for d, h in zip(sset["di"], sset["hi"]):
+                d.copy_(h, non_blocking=True)
+            for d, h in zip(sset["df"], sset["hf"]):
+                h.copy_(d, non_blocking=True)
+    ctrials = []
+    for _ in range(3):
+        _barrier(ws)
+        t0 = time.perf_counter()
+        for k in range(steps):
+            copy_step(k)
+        torch.cuda.synchronize()
+        ctrials.append(_allreduce_max((time.perf_counter() - t0) / steps, ws))
+    t_copies = sorted(ctrials)[1]
+
     # zero copy: the layouts point at the pinned host arenas themselves; the
     # kernel reads and writes them over the host link, no staging copies
     s0 = sets[0]
     zI, zF = _desc_array(w.inits, s0["hi"], keep), _desc_array(w.finals, s0["hf"], keep)
     zp = C.c_void_p()
     capi.check(lib.g2g_plan_create_batch(n, zI, zF, dts, ops, sp0, C.byref(zp)))
-    capi.check(lib.g2g_plan_execute(zp, sp0))
+    for _k in range(max(1, steps)):
+        capi.check(lib.g2g_plan_execute(zp, sp0))
     s0["stream"].synchronize()
     ztrials = []
     for _ in range(3):
@@ -749,6 +770,11 @@ def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
             "trials_ms_per_step": [round(t * 1e3, 3) for t in trials],
             "path": "pinned host arenas -> H2D -> g2g_plan_execute -> D2H, two steps in "
                     "flight on two streams",
+            "copies_only": {"ms_per_step": round(t_copies * 1e3, 3),
+                            "link_gbs": round((h2d + d2h) / t_copies / 1e9, 1),
+                            "frac": round(t_copies / t_pipe, 4),
+                            "path": "the same H2D and D2H copies without the transform "
+                                    "(the host-link bound of a step)"},
             "sequential": {"value": round(w.bytes_moved * ws / t_seq / 1e9, 3),
                            "ms_per_step": round(t_seq * 1e3, 3),
                            "path": "pinned host arenas -> H2D -> g2g_transform_batch "
