@@ -385,9 +385,10 @@ def run_ours(args):
     capi.check(lib.g2g_plan_destroy(plan))
 
     # the scaled form on the same layouts: final = 0.5*final + 2*initial
-    scaled = None
+    scaled = cast = None
     if args.batch and rank == 0 and w.ops is None:
         scaled = run_scaled(lib, w, dI, dF, dts, stream, peak, args.steps // 4 or 1)
+        cast = run_cast(lib, dev, stream, peak, args.steps // 4 or 1)
 
     batched = serving = None
     if args.batch and rank == 0:
@@ -416,7 +417,7 @@ def run_ours(args):
             "data": "synthetic (seeded random bit patterns, device-resident)",
             "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
-            "batched_stream": batched, "serving": serving, "scaled": scaled,
+            "batched_stream": batched, "serving": serving, "scaled": scaled, "cast": cast,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
                      "tuning": {k: getattr(info.tuning, k) for k in
@@ -483,6 +484,55 @@ def run_scaled(lib, w, dI, dF, dts, stream, peak, steps):
             "value": round(info.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
             "traffic_bytes": info.bytes_min_traffic,
             "roofline_frac": round(info.bytes_min_traffic / (ms * 1e-3) / 1e9 / peak, 4)}
+
+
+def run_cast(lib, dev, stream, peak, steps, m=16384):
+    """The fused dtype cast on random grid layouts of the headline's kind
+    (16 virtual ranks, splits U[1,2048], padded strides): float32 -> float64
+    and back. Traffic per element: sizeof(src) + sizeof(dst)."""
+    import torch
+    from grid2grid_gb300 import capi
+    from grid2grid_gb300 import layouts as Ls
+    rng = np.random.default_rng(2024)
+    L32 = Ls.random_grid_layout(m, m, 16, capi.FLOAT32, rng)
+    L64 = Ls.random_grid_layout(m, m, 16, capi.FLOAT64, rng)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(99)
+    # float32 arena: finite normals; float64 arena: float64 normals
+    a32 = torch.randn(L32.arena_bytes // 4, generator=gen, device=dev).view(torch.uint8)
+    a64 = torch.randn(L64.arena_bytes // 8, generator=gen, device=dev,
+                      dtype=torch.float64).view(torch.uint8)
+    keep = []
+    d32 = _desc_array([L32], [a32], keep)
+    d64 = _desc_array([L64], [a64], keep)
+    sp = C.c_void_p(stream.cuda_stream)
+    out = {"layouts": "random grids 16384^2, 16 ranks, splits U[1,2048], padded strides"}
+    for name, (di, dts, df, dtd) in {"f32_to_f64": (d32, capi.FLOAT32, d64, capi.FLOAT64),
+                                     "f64_to_f32": (d64, capi.FLOAT64, d32, capi.FLOAT32)}.items():
+        plan = C.c_void_p()
+        capi.check(lib.g2g_plan_create_cast(di, dts, df, dtd, None, sp, C.byref(plan)))
+        info = capi.PlanInfo()
+        capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
+        ms = _time_steps(stream, lambda: capi.check(lib.g2g_plan_execute(plan, sp)), steps, 3)
+        capi.check(lib.g2g_plan_destroy(plan))
+        out[name] = {"ms_per_step": round(ms, 4),
+                     "value": round(info.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
+                     "traffic_bytes": info.bytes_min_traffic,
+                     "roofline_frac": round(info.bytes_min_traffic / (ms * 1e-3) / 1e9 / peak, 4)}
+    del a32, a64
+    return out
+
+
+def run_cast_only(args):
+    import torch
+    from grid2grid_gb300 import capi
+    lib = capi.load()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    peak, _ = _peaks()
+    print(json.dumps({"cast": run_cast(lib, dev, stream, peak, args.steps)}))
+    return 0
 
 
 def run_batched(lib, dev, stream, steps, peak):
@@ -796,6 +846,9 @@ def main(argv=None):
                     default=None, metavar="A,B",
                     help="time final = B*final + A*op(initial) on the workload instead "
                          "of its plain transform (the scaled kernel instances)")
+    ap.add_argument("--cast-only", action="store_true",
+                    help="time only the fused dtype casts (float32 <-> float64 on random "
+                         "grids) and print their figures (the cast kernel instances)")
     ap.add_argument("--no-batch", dest="batch", action="store_false",
                     help="skip the 256-transform batched stream")
     ap.add_argument("--no-serving", dest="serving", action="store_false",
@@ -804,6 +857,8 @@ def main(argv=None):
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.cast_only:
+        return run_cast_only(args)
     return run_ours(args)
 
 

@@ -53,37 +53,80 @@ def _expected(Li, Lf, ai, af, src, dst, trans):
     return out
 
 
-def _layouts(rng, src, dst, trans, m=257, n=190, P=5):
+def _comp(dt):
+    """Bytes of the real component: the alignment an element address needs."""
+    return 8 if dt in (capi.FLOAT64, capi.COMPLEX128) else 4
+
+
+def _layouts(rng, src, dst, trans, m=257, n=190, P=5, ext_hi=70, mis=(0, 0)):
+    """mis: byte offsets of every initial / final block past an aligned
+    address (rounded down to the component alignment of each side)."""
     Li = Ls.random_grid_layout(m if trans == "N" else n, n if trans == "N" else m, P, src, rng,
-                               ext_hi=70)
-    Lf = Ls.random_grid_layout(m, n, P, dst, rng, ext_hi=70)
+                               ext_hi=ext_hi, byte_misalign=mis[0] - mis[0] % _comp(src))
+    Lf = Ls.random_grid_layout(m, n, P, dst, rng, ext_hi=ext_hi,
+                               byte_misalign=mis[1] - mis[1] % _comp(dst))
     return Li, Lf
+
+
+def _check_cast(rng, Li, Lf, src, dst, trans, where=("device", "device")):
+    import torch
+    ai = _values(rng, Li, src)
+    af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
+    Lt = Li.copy().transpose_or_conjugate(trans) if trans != "N" else Li
+    want = _expected(Lt, Lf, ai, af, src, dst, trans)
+    lib = capi.load()
+
+    def place(a, w):
+        if w == "device":
+            return T.to_device([a])[0]
+        t = torch.empty(len(a), dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = a
+        return t
+    di, df = place(ai, where[0]), place(af, where[1])
+    dI, k1 = Li.desc(di.data_ptr())
+    dF, k2 = Lf.desc(df.data_ptr())
+    op = capi.make_op(trans, 1.0, 0.0)
+    capi.check(lib.g2g_transform_cast(C.byref(dI), src, C.byref(dF), dst, C.byref(op), None))
+    torch.cuda.synchronize()
+    got = df.cpu().numpy().copy()
+    Lcmp = Ls.Layout(Lf.rows_split, Lf.cols_split, Lf.owners, Lf.n_ranks,
+                     capi.FLOAT64 if _comp(dst) == 8 else capi.FLOAT32, [], [], [], [], [], 0)
+    T.assert_arenas_equal(got, want, Lcmp, nan_equivalent=True,
+                          what=f"cast {src}->{dst} op {trans} {where}")
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("src,dst", CASTS)
 @pytest.mark.parametrize("trans", ["N", "T", "C"])
 def test_cast_matches_numpy(src, dst, trans):
-    import torch
     rng = np.random.default_rng(100 * src + 10 * dst + "NTC".index(trans))
     Li, Lf = _layouts(rng, src, dst, trans)
-    ai = _values(rng, Li, src)
-    af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
-    Lt = Li.copy().transpose_or_conjugate(trans) if trans != "N" else Li
-    want = _expected(Lt, Lf, ai, af, src, dst, trans)
-    lib = capi.load()
-    di, df = T.to_device([ai, af])
-    dI, k1 = Li.desc(di.data_ptr())
-    dF, k2 = Lf.desc(df.data_ptr())
-    op = capi.make_op(trans, 1.0, 0.0)
-    capi.check(lib.g2g_transform_cast(C.byref(dI), src, C.byref(dF), dst, C.byref(op), None))
-    torch.cuda.synchronize()
-    got = df.cpu().numpy()
-    comp = 8 if dst in (capi.FLOAT64, capi.COMPLEX128) else 4
-    Lcmp = Ls.Layout(Lf.rows_split, Lf.cols_split, Lf.owners, Lf.n_ranks,
-                     capi.FLOAT64 if comp == 8 else capi.FLOAT32, [], [], [], [], [], 0)
-    T.assert_arenas_equal(got, want, Lcmp, nan_equivalent=True,
-                          what=f"cast {src}->{dst} op {trans}")
+    _check_cast(rng, Li, Lf, src, dst, trans)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("src,dst", CASTS)
+@pytest.mark.parametrize("mis", [(0, 4), (4, 8), (8, 12)])
+def test_cast_long_columns_and_misaligned_blocks(src, dst, mis):
+    """Columns of up to 700 rows (tiles of several 16-byte chunks per column,
+    staged through shared memory), pieces of many short columns (tiles too
+    wide to stage), blocks at 4, 8 or 12 bytes past a 16-byte boundary
+    (destination elements that straddle 16-byte chunks)."""
+    rng = np.random.default_rng(1000 * src + 100 * dst + mis[0] + mis[1])
+    Li, Lf = _layouts(rng, src, dst, "N", m=1500, n=1200, P=7, ext_hi=700, mis=mis)
+    _check_cast(rng, Li, Lf, src, dst, "N")
+    Li, Lf = _layouts(rng, src, dst, "N", m=40, n=2600, P=3, ext_hi=2000, mis=mis)
+    _check_cast(rng, Li, Lf, src, dst, "N")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("where", [("host", "device"), ("device", "host")])
+def test_cast_host_memory(where):
+    """Layouts in pinned host memory: the cast reads / writes them in place."""
+    rng = np.random.default_rng(41)
+    for src, dst in [(capi.FLOAT32, capi.FLOAT64), (capi.COMPLEX128, capi.COMPLEX64)]:
+        Li, Lf = _layouts(rng, src, dst, "N", m=600, n=300, ext_hi=400)
+        _check_cast(rng, Li, Lf, src, dst, "N", where)
 
 
 def test_cast_argument_checks():
