@@ -525,16 +525,16 @@ void assemble(g2g_plan &pl) {
         pi.cells = pl.n_cells;
         pl.n_cells += cells;
         pl.max_cells_per_pair = std::max(pl.max_cells_per_pair, cells);
-        // scaled tiles are warp-level when no destination element straddles
-        // a 16-byte chunk: every final block starts on a multiple of
-        // min(sizeof(T), 16) bytes (column and row offsets keep that)
+        // scaled and cast tiles are warp-level when no destination element
+        // straddles a 16-byte chunk: every final block starts on a multiple
+        // of min(sizeof(T), 16) bytes (column and row offsets keep that)
         bool dst_chunked = true;
         for (const HBlock &b : p.b.blocks)
             dst_chunked = dst_chunked && b.data % (uint64_t)std::min(p.esz, 16) == 0;
-        const bool warp_scaled = p.scaled && !p.cast && dst_chunked;
+        const bool warp_elem = (p.scaled || p.cast) && dst_chunked;
         pi.kind = esz_code(p.esz) | ((uint32_t)p.dtype << g2g::KIND_DTYPE_SHIFT) |
                   (p.scaled ? g2g::KIND_SCALED : 0u) |
-                  (warp_scaled ? g2g::KIND_WARP_SCALED : 0u) |
+                  (warp_elem ? g2g::KIND_WARP_ELEM : 0u) |
                   (p.cast ? (g2g::KIND_CAST |
                              ((uint32_t)p.src_dtype << g2g::KIND_SRC_DTYPE_SHIFT))
                           : 0u);
@@ -564,10 +564,10 @@ void assemble(g2g_plan &pl) {
             if (!b.trans)
                 any_plain = true;
         if (p.cast)
-            pl.paths |= 16;
+            pl.paths |= 16 | (warp_elem && any_plain ? 1 : 0);
         else if (p.scaled) // real and complex arithmetic are separate kernel paths
             pl.paths |= ((p.dtype == G2G_COMPLEX64 || p.dtype == G2G_COMPLEX128) ? 8 : 4) |
-                        (warp_scaled && any_plain ? 1 : 0);
+                        (warp_elem && any_plain ? 1 : 0);
         else
             pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0);
     }

@@ -26,9 +26,9 @@ enum : uint32_t {
     KIND_CONJ = 0x8u,       // flip the sign of the imaginary part
     KIND_SCALED = 0x10u,    // dst = beta*dst + alpha*src instead of a copy
     KIND_CAST = 0x20u,      // source elements of another type, converted
-    KIND_WARP_SCALED = 0x40u, // with KIND_SCALED: every destination element lies
-                              // inside one 16-byte chunk, so non-transposed
-                              // tiles are warp-level work items
+    KIND_WARP_ELEM = 0x40u, // with KIND_SCALED or KIND_CAST: every destination
+                            // element lies inside one 16-byte chunk, so
+                            // non-transposed tiles are warp-level work items
     KIND_DTYPE_SHIFT = 8u,  // g2g_dtype in bits 8-9 (the destination's)
     KIND_SRC_DTYPE_SHIFT = 10u, // with KIND_CAST: the source's g2g_dtype, bits 10-11
 };

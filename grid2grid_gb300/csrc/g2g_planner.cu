@@ -120,14 +120,14 @@ __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
     }
 }
 
-// Plain copies and non-transposed scaled tiles whose destination elements
-// never straddle a 16-byte chunk are warp-level work items, the other
-// transposed, scaled and converting tiles CTA-level ones; the work list holds
-// all warp-level tiles first.
+// Plain copies, and non-transposed scaled or converting tiles whose
+// destination elements never straddle a 16-byte chunk, are warp-level work
+// items; the other (transposed, scaled, converting) tiles CTA-level ones.
+// The work list holds all warp-level tiles first.
 __device__ inline bool is_copy_kind(uint32_t kind) {
-    if (kind & (KIND_TRANS | KIND_CAST))
+    if (kind & KIND_TRANS)
         return false;
-    return !(kind & KIND_SCALED) || (kind & KIND_WARP_SCALED);
+    return !(kind & (KIND_SCALED | KIND_CAST)) || (kind & KIND_WARP_ELEM);
 }
 
 __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pairs,

@@ -55,13 +55,22 @@ int stage_bytes_for(int tile_bytes) {
 
 size_t ring_smem_bytes(const ScatterConfig &cfg) {
     const int u = cfg.unroll == 1 ? 1 : (cfg.unroll == 2 ? 2 : 4);
-    // kernels with scaled tiles stage destination chunks as well
-    const size_t per_warp =
-        (cfg.paths & PATH_SCALED)
-            ? (size_t)(u == 1 ? ring_warp_bytes<1, true>()
-                              : (u == 2 ? ring_warp_bytes<2, true>() : ring_warp_bytes<4, true>()))
-            : (size_t)(u == 1 ? ring_warp_bytes<1, false>()
-                              : (u == 2 ? ring_warp_bytes<2, false>() : ring_warp_bytes<4, false>()));
+    // kernels with scaled tiles stage destination chunks as well, kernels
+    // with cast tiles up to three source blocks per chunk
+    size_t per_warp = 0;
+    switch (ring_extra_rows(cfg.paths)) {
+    case 1:
+        per_warp = u == 1 ? ring_warp_bytes<1, 1>()
+                          : (u == 2 ? ring_warp_bytes<2, 1>() : ring_warp_bytes<4, 1>());
+        break;
+    case 2:
+        per_warp = u == 1 ? ring_warp_bytes<1, 2>()
+                          : (u == 2 ? ring_warp_bytes<2, 2>() : ring_warp_bytes<4, 2>());
+        break;
+    default:
+        per_warp = u == 1 ? ring_warp_bytes<1, 0>()
+                          : (u == 2 ? ring_warp_bytes<2, 0>() : ring_warp_bytes<4, 0>());
+    }
     const size_t ring = (size_t)(cfg.threads / 32) * per_warp;
     return ring > cfg.trans_bytes ? ring : cfg.trans_bytes;
 }

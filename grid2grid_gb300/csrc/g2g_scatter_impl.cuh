@@ -362,7 +362,7 @@ __device__ __forceinline__ int staged_pitch(int L) { return ((L + 15) & ~15) + 1
 // Plain tiles whose columns are long enough for bulk copies to pay off and
 // whose columns fit one stage.
 __device__ __forceinline__ bool tma_eligible(const Tile &t, int stage_bytes) {
-    if (t.kind & (KIND_TRANS | KIND_SCALED))
+    if (t.kind & (KIND_TRANS | KIND_SCALED | KIND_CAST))
         return false;
     const int L = t.rows * kind_esz(t.kind);
     return L >= 256 && (long long)t.cols * staged_pitch(L) <= (long long)stage_bytes;
@@ -1177,8 +1177,10 @@ __device__ __forceinline__ void scaled_transpose_store(const Tile &t, const Pair
 // complex<float> <-> complex<double> round each part to nearest (the CUDA
 // conversion intrinsics, IEEE round-to-nearest-even); real -> complex sets
 // the imaginary part to +0; 'C' flips the imaginary sign after the
-// conversion. CTA-wide: non-transposed tiles walk columns (warps) and rows
-// (lanes, four elements in flight each); transposed ones go through a padded
+// conversion. Non-transposed tiles whose destination elements sit whole in
+// 16-byte chunks run on the copy ring (ring_store_cast); the others are
+// CTA-wide: non-transposed ones walk columns (warps) and rows (lanes, four
+// elements in flight each), transposed ones go through a padded
 // shared-memory tile of destination elements.
 __device__ __forceinline__ float cvt(float v, float *) { return v; }
 __device__ __forceinline__ double cvt(float v, double *) { return (double)v; }
@@ -1200,31 +1202,42 @@ template <typename D, typename S> __device__ __forceinline__ D convert(S v) {
     return cvt(v, (D *)nullptr);
 }
 
+// A non-transposed cast tile element by element, columns over NWARP warps
+// (warp `warp` of them), four elements in flight per lane.
 // (one function per conversion, called per tile: the kernel does not carry
 // the registers of all twelve)
+template <int NWARP, typename S, typename D>
+__device__ __noinline__ void cast_cols(const Tile &t, int warp) {
+    constexpr int ES = (int)sizeof(S), ED = (int)sizeof(D);
+    const int lane = threadIdx.x & 31;
+    const int R = t.rows, Cn = t.cols;
+    for (int c = warp; c < Cn; c += NWARP) {
+        const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
+        const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+        for (int r0 = lane; r0 < R; r0 += 32 * 4) {
+            S v[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (r0 + 32 * k < R)
+                    v[k] = ld_elem<S>(sc + (uint64_t)(r0 + 32 * k) * ES);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (r0 + 32 * k < R)
+                    st_elem<D>(dc + (uint64_t)(r0 + 32 * k) * ED, convert<D>(v[k]));
+        }
+    }
+}
+
 template <int THREADS, typename S, typename D>
 __device__ __noinline__ void cast_tile(const Tile &t, unsigned char *smem_raw, int td) {
     constexpr int NWARP = THREADS / 32;
-    constexpr int ES = (int)sizeof(S), ED = (int)sizeof(D);
+    constexpr int ED = (int)sizeof(D);
+    constexpr int ES = (int)sizeof(S);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool conj = (t.kind & KIND_CONJ) != 0;
     const int R = t.rows, Cn = t.cols;
     if (!(t.kind & KIND_TRANS)) {
-        for (int c = warp; c < Cn; c += NWARP) {
-            const uint64_t sc = t.src + (uint64_t)((long long)c * t.src_ld);
-            const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
-            for (int r0 = lane; r0 < R; r0 += 32 * 4) {
-                S v[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (r0 + 32 * k < R)
-                        v[k] = ld_elem<S>(sc + (uint64_t)(r0 + 32 * k) * ES);
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (r0 + 32 * k < R)
-                        st_elem<D>(dc + (uint64_t)(r0 + 32 * k) * ED, convert<D>(v[k]));
-            }
-        }
+        cast_cols<NWARP, S, D>(t, warp);
         return;
     }
     D *smem = reinterpret_cast<D *>(smem_raw);
@@ -1408,8 +1421,35 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
 
 // A warp-level work item on the register path: a plain copy, or (kernels
 // with scaled tiles) a non-transposed scaled tile, by NWARP warps.
+template <int NWARP, typename S>
+__device__ __forceinline__ void cast_cols_to(const Tile &t, int warp) {
+    switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0:
+        if constexpr (!is_cplx<S>::value)
+            cast_cols<NWARP, S, float>(t, warp);
+        break;
+    case 1:
+        if constexpr (!is_cplx<S>::value)
+            cast_cols<NWARP, S, double>(t, warp);
+        break;
+    case 2: cast_cols<NWARP, S, cplxf>(t, warp); break;
+    default: cast_cols<NWARP, S, cplxd>(t, warp); break;
+    }
+}
+
 template <int NWARP, int U, int PATHS>
 __device__ __forceinline__ void warp_tile(const Tile &t, int warp, const PairInfo *pairs) {
+    if constexpr ((PATHS & PATH_CAST) != 0) {
+        if (t.kind & KIND_CAST) {
+            switch ((t.kind >> KIND_SRC_DTYPE_SHIFT) & 3u) {
+            case 0: cast_cols_to<NWARP, float>(t, warp); break;
+            case 1: cast_cols_to<NWARP, double>(t, warp); break;
+            case 2: cast_cols_to<NWARP, cplxf>(t, warp); break;
+            default: cast_cols_to<NWARP, cplxd>(t, warp); break;
+            }
+            return;
+        }
+    }
     if constexpr ((PATHS & PATH_SCALED) != 0) {
         if (t.kind & KIND_SCALED) {
             switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
@@ -1501,16 +1541,20 @@ constexpr int RING_OPT_RUN_MASK = 0xff;
 constexpr int RING_OPT_L2_PREFETCH = 0x100;
 static_assert(sizeof(Tile) <= RING_QE, "a Tile fits a queue entry");
 
-// Per-warp shared memory: RING_D stages of 32U + 1 source blocks (and, in
-// kernels with scaled tiles, the 32U destination chunks they update), the
-// descriptor queue, one valid flag per stage (0: no stage, the warp's work is
-// done).
-template <int U, bool SC> __host__ __device__ constexpr int ring_stage_bytes() {
-    return (U * 32 + 1) * 16 + (SC ? U * 32 * 16 : 0);
+// Per-warp shared memory: RING_D stages of 32U + 1 source blocks plus XR
+// extra rows of 32U blocks (kernels with scaled tiles: one row, the
+// destination chunks they update; with cast tiles: two rows, a chunk's second
+// and third source blocks), the descriptor queue, one valid flag per stage
+// (0: no stage, the warp's work is done).
+template <int U, int XR> __host__ __device__ constexpr int ring_stage_bytes() {
+    return (U * 32 + 1) * 16 + XR * U * 32 * 16;
 }
-template <int U, bool SC> __host__ __device__ constexpr int ring_warp_bytes() {
-    return RING_D * ring_stage_bytes<U, SC>() + RING_Q * RING_QE +
+template <int U, int XR> __host__ __device__ constexpr int ring_warp_bytes() {
+    return RING_D * ring_stage_bytes<U, XR>() + RING_Q * RING_QE +
            ((RING_D * 4 + 15) / 16) * 16;
+}
+__host__ __device__ constexpr int ring_extra_rows(int paths) {
+    return (paths & PATH_SCALED) ? 1 : ((paths & PATH_CAST) ? 2 : 0);
 }
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
@@ -1523,7 +1567,12 @@ __device__ __forceinline__ void cp_async_commit() {
 template <int N> __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
-// a ring read, ordered after the wait and warp barrier that make it valid
+// ring reads, ordered after the wait and warp barrier that make them valid
+__device__ __forceinline__ uint32_t lds_ring_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
 __device__ __forceinline__ uint4 lds_ring(uint32_t a) {
     uint4 v;
     asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
@@ -1541,8 +1590,10 @@ struct RingTile {
     int cols, L, cpc, dq, dr, total;
     float rcp; // 1 / cpc, for the quotients of small numbers by cpc
     bool aligned;
-    uint32_t kind; // KIND_SCALED: beta*dst + alpha*src (dtype in the kind)
+    uint32_t kind; // KIND_SCALED: beta*dst + alpha*src (dtype in the kind);
+                   // KIND_CAST: converted elements (both dtypes in the kind)
     int pair;
+    int edsh, essh; // cast tiles: log2 of the destination / source element sizes
 };
 __device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
     c.kind = t.kind;
@@ -1554,7 +1605,15 @@ __device__ __forceinline__ void ring_tile_init(RingTile &c, const Tile &t) {
     c.cols = t.cols;
     c.L = t.rows * kind_esz(t.kind);
     c.aligned = (((t.src - t.dst) | (uint64_t)(t.src_ld - t.dst_ld)) & 15u) == 0;
-    if (((t.dst_ld | t.src_ld) & 15) == 0) {
+    if (t.kind & KIND_CAST) {
+        const uint32_t sdt = (t.kind >> KIND_SRC_DTYPE_SHIFT) & 3u; // f32, f64, c64, c128
+        c.edsh = 2 + (int)(t.kind & KIND_ESZ_MASK);
+        c.essh = 2 + (sdt != 0u ? 1 : 0) + (sdt == 3u ? 1 : 0);
+        // a cast chunk fetches its own source blocks: the walk counts the
+        // destination chunks a column touches (the lead d0 is at most 12)
+        c.cpc = (t.dst_ld & 15) == 0 ? (int)(((t.dst & 15u) + (uint64_t)c.L + 15u) >> 4)
+                                     : ((c.L + 27) >> 4);
+    } else if (((t.dst_ld | t.src_ld) & 15) == 0) {
         const int d0 = (int)(t.dst & 15u);
         const int sh = (int)((t.src - (uint64_t)d0) & 15u);
         c.cpc = (sh + d0 + c.L + 15) >> 4;
@@ -1595,14 +1654,206 @@ __device__ __forceinline__ void ring_walk_step(RingWalk &w, const RingTile &c) {
     }
 }
 
+// Cast tiles on the ring (destination elements whole within each 16-byte
+// chunk): the walk runs over destination chunks; the chunk of lane i in step
+// u needs source elements [jlo, jhi) of its column, at most 32 bytes, which
+// lie in at most three aligned source blocks, staged in rows 0, 1 and 2 of
+// slot u * 32 + i. The storing side converts them into the chunk.
+struct CastSpan {
+    int jlo, jhi, j0; // elements in the chunk, j0 the first element slot (may be < 0)
+    int first;        // byte of element jlo from the column's aligned source base
+    int nblk;         // source blocks (0: the chunk holds no destination bytes)
+};
+// edsh / essh: log2 of the destination / source element sizes
+__device__ __forceinline__ CastSpan cast_span(const RingTile &c, const RingWalk &w, int edsh,
+                                              int essh) {
+    CastSpan p;
+    const int d0 = (int)(w.d & 15u);
+    const int relb = (w.k << 4) - d0; // chunk start from the column start, bytes
+    p.nblk = 0;
+    p.j0 = relb >> edsh; // exact: d0 is a multiple of the element size
+    p.jlo = relb < 0 ? 0 : p.j0;
+    p.jhi = (relb + 16 < c.L ? relb + 16 : c.L) >> edsh;
+    p.first = 0;
+    if (w.col < c.cols && relb < c.L && relb + 16 > 0) {
+        const int s0 = (int)(w.s & 15u);
+        p.first = s0 + (p.jlo << essh);
+        p.nblk = ((s0 + (p.jhi << essh) - 1) >> 4) - (p.first >> 4) + 1;
+    }
+    return p;
+}
+template <int U>
+__device__ __forceinline__ void ring_issue_cast(const RingTile &c, RingWalk &w, uint32_t slots,
+                                                int lane) {
+    constexpr uint32_t ROW1 = (U * 32 + 1) * 16, ROW = U * 32 * 16;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const CastSpan p = cast_span(c, w, c.edsh, c.essh);
+        const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+        const uint64_t a0 = (w.s & ~15ull) + (uint64_t)(p.first & ~15);
+        if (p.nblk > 0)
+            cp_async16(slot, a0);
+        if (p.nblk > 1)
+            cp_async16(slot + ROW1, a0 + 16);
+        if (p.nblk > 2)
+            cp_async16(slot + ROW1 + ROW, a0 + 32);
+        ring_walk_step(w, c);
+    }
+}
+// Word of the staged source window at byte `o` from its first block.
+template <int U>
+__device__ __forceinline__ uint32_t cast_word(uint32_t slot, int o) {
+    constexpr uint32_t ROW1 = (U * 32 + 1) * 16, ROW = U * 32 * 16;
+    const int q = o >> 4;
+    return lds_ring_u32(slot + (q == 0 ? 0u : (q == 1 ? ROW1 : ROW1 + ROW)) + (uint32_t)(o & 15));
+}
+// A source element of the staged window at byte `o` (its words may lie in
+// two consecutive blocks).
+template <int U, typename S> struct CastSrc;
+template <int U> struct CastSrc<U, float> {
+    static __device__ __forceinline__ float get(uint32_t slot, int o) {
+        return __uint_as_float(cast_word<U>(slot, o));
+    }
+};
+template <int U> struct CastSrc<U, double> {
+    static __device__ __forceinline__ double get(uint32_t slot, int o) {
+        return dbl(cast_word<U>(slot, o), cast_word<U>(slot, o + 4));
+    }
+};
+template <int U> struct CastSrc<U, cplxf> {
+    static __device__ __forceinline__ cplxf get(uint32_t slot, int o) {
+        return cplxf{__uint_as_float(cast_word<U>(slot, o)),
+                     __uint_as_float(cast_word<U>(slot, o + 4))};
+    }
+};
+template <int U> struct CastSrc<U, cplxd> {
+    static __device__ __forceinline__ cplxd get(uint32_t slot, int o) {
+        return cplxd{dbl(cast_word<U>(slot, o), cast_word<U>(slot, o + 4)),
+                     dbl(cast_word<U>(slot, o + 8), cast_word<U>(slot, o + 12))};
+    }
+};
+// A source element from its words.
+template <typename S> __device__ __forceinline__ S src_words(const uint32_t *w);
+template <> __device__ __forceinline__ float src_words<float>(const uint32_t *w) {
+    return __uint_as_float(w[0]);
+}
+template <> __device__ __forceinline__ double src_words<double>(const uint32_t *w) {
+    return dbl(w[0], w[1]);
+}
+template <> __device__ __forceinline__ cplxf src_words<cplxf>(const uint32_t *w) {
+    return cplxf{__uint_as_float(w[0]), __uint_as_float(w[1])};
+}
+template <> __device__ __forceinline__ cplxd src_words<cplxd>(const uint32_t *w) {
+    return cplxd{dbl(w[0], w[1]), dbl(w[2], w[3])};
+}
+// A converted element as destination words.
+template <typename D> __device__ __forceinline__ void put_words(uint32_t *w, D v);
+template <> __device__ __forceinline__ void put_words<float>(uint32_t *w, float v) {
+    w[0] = __float_as_uint(v);
+}
+template <> __device__ __forceinline__ void put_words<double>(uint32_t *w, double v) {
+    dbl_words(v, w[0], w[1]);
+}
+template <> __device__ __forceinline__ void put_words<cplxf>(uint32_t *w, cplxf v) {
+    w[0] = __float_as_uint(v.x);
+    w[1] = __float_as_uint(v.y);
+}
+template <> __device__ __forceinline__ void put_words<cplxd>(uint32_t *w, cplxd v) {
+    dbl_words(v.x, w[0], w[1]);
+    dbl_words(v.y, w[2], w[3]);
+}
+// Stores one landed stage of a cast tile: each chunk's elements converted,
+// whole chunks with one 16-byte store, head and tail chunks by element.
+template <int U, typename S, typename D>
+__device__ __forceinline__ void ring_store_cast(const RingTile &c, RingWalk &w, uint32_t slots,
+                                                int lane) {
+    constexpr int ES = (int)sizeof(S), ED = (int)sizeof(D), EPC = 16 / ED;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        constexpr int EDSH = ED == 4 ? 2 : (ED == 8 ? 3 : 4);
+        constexpr int ESSH = ES == 4 ? 2 : (ES == 8 ? 3 : 4);
+        const CastSpan p = cast_span(c, w, EDSH, ESSH);
+        if (p.nblk > 0) {
+            const uint32_t slot = slots + (uint32_t)((u * 32 + lane) << 4);
+            // byte of element 0 in the staged window (may be < 0)
+            const int o0 = (int)(w.s & 15u) - (p.first & ~15);
+            const uint64_t chunk = w.d - (w.d & 15u) + (uint64_t)(w.k << 4);
+            if (p.jlo == p.j0 && p.jhi == p.j0 + EPC) {
+                // the chunk's source bytes from word q of the first block on,
+                // gathered from the rows with 16-byte reads
+                constexpr uint32_t ROW1 = (U * 32 + 1) * 16, ROW = U * 32 * 16;
+                const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+                const uint32_t q = (uint32_t)((p.first & 15) >> 2);
+                const uint4 r0 = lds_ring(slot);
+                const uint4 r1 = p.nblk > 1 ? lds_ring(slot + ROW1) : zero;
+                const uint4 w0 = funnel_words(r0, r1, q);
+                uint32_t sw[8] = {w0.x, w0.y, w0.z, w0.w, 0u, 0u, 0u, 0u};
+                if constexpr (EPC * ES > 16) {
+                    const uint4 r2 = p.nblk > 2 ? lds_ring(slot + ROW1 + ROW) : zero;
+                    const uint4 w1 = funnel_words(r1, r2, q);
+                    sw[4] = w1.x;
+                    sw[5] = w1.y;
+                    sw[6] = w1.z;
+                    sw[7] = w1.w;
+                }
+                uint32_t x[4];
+#pragma unroll
+                for (int e = 0; e < EPC; ++e)
+                    put_words<D>(x + e * (ED / 4), convert<D>(src_words<S>(sw + e * (ES / 4))));
+                st_v4(chunk, make_uint4(x[0], x[1], x[2], x[3]));
+            } else {
+#pragma unroll
+                for (int e = 0; e < EPC; ++e) {
+                    const int j = p.j0 + e;
+                    if (j >= p.jlo && j < p.jhi)
+                        st_elem<D>(chunk + (uint64_t)(e * ED),
+                                   convert<D>(CastSrc<U, S>::get(slot, o0 + j * ES)));
+                }
+            }
+        }
+        ring_walk_step(w, c);
+    }
+}
+template <int U, typename S>
+__device__ __forceinline__ void ring_store_cast_to(const RingTile &c, RingWalk &w,
+                                                   uint32_t slots, int lane) {
+    switch ((c.kind >> KIND_DTYPE_SHIFT) & 3u) {
+    case 0:
+        if constexpr (!is_cplx<S>::value)
+            ring_store_cast<U, S, float>(c, w, slots, lane);
+        break;
+    case 1:
+        if constexpr (!is_cplx<S>::value)
+            ring_store_cast<U, S, double>(c, w, slots, lane);
+        break;
+    case 2: ring_store_cast<U, S, cplxf>(c, w, slots, lane); break;
+    default: ring_store_cast<U, S, cplxd>(c, w, slots, lane); break;
+    }
+}
+template <int U>
+__device__ __forceinline__ void ring_store_cast_dispatch(const RingTile &c, RingWalk &w,
+                                                         uint32_t slots, int lane) {
+    switch ((c.kind >> KIND_SRC_DTYPE_SHIFT) & 3u) {
+    case 0: ring_store_cast_to<U, float>(c, w, slots, lane); break;
+    case 1: ring_store_cast_to<U, double>(c, w, slots, lane); break;
+    case 2: ring_store_cast_to<U, cplxf>(c, w, slots, lane); break;
+    default: ring_store_cast_to<U, cplxd>(c, w, slots, lane); break;
+    }
+}
 // Issues the cp.async copies of one stage into ring slots `slots`; for a
 // scaled tile (SC kernels) also the destination chunks, after the source
 // blocks. Only this lane's own destination words of a chunk are ever stored,
 // and no other work item writes them, so the chunk's other words may be stale.
-template <int U, bool SC>
+template <int U, int PATHS>
 __device__ __forceinline__ void ring_issue(const RingTile &c, RingWalk &w, uint32_t slots,
                                            int lane) {
-    const bool scaled = SC && (c.kind & KIND_SCALED);
+    if constexpr ((PATHS & PATH_CAST) != 0) {
+        if (c.kind & KIND_CAST) {
+            ring_issue_cast<U>(c, w, slots, lane);
+            return;
+        }
+    }
+    const bool scaled = (PATHS & PATH_SCALED) && (c.kind & KIND_SCALED);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         if (w.col < c.cols) {
@@ -1760,8 +2011,9 @@ __device__ __forceinline__ void ring_prefetch_tile(const RingTile &c, const Ring
                                                    int lane) {
     if (!o.l2_prefetch || c.total <= 32 * U || c.L < 256 || lane >= c.cols)
         return;
+    const int Ls = (c.kind & KIND_CAST) ? c.L / kind_esz(c.kind) * kind_src_esz(c.kind) : c.L;
     const uint64_t s = c.src + (uint64_t)((long long)lane * c.sld);
-    const uint64_t start = s & ~15ull, end = (s + (uint64_t)c.L + 15u) & ~15ull;
+    const uint64_t start = s & ~15ull, end = (s + (uint64_t)Ls + 15u) & ~15ull;
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(start),
                  "r"((uint32_t)(end - start))
                  : "memory");
@@ -1778,7 +2030,7 @@ struct RingIssue {
 };
 
 // Fills ring stage `st` from the issuing cursor (or marks it empty) and commits it.
-template <int U, bool SC>
+template <int U, int PATHS>
 __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
                                           const RingOrder &ord, uint32_t slots,
                                           const unsigned char *queue, uint32_t queue_s,
@@ -1786,7 +2038,7 @@ __device__ __forceinline__ void ring_fill(const PlanList &list, RingIssue &q,
     if (q.ti < list.total_copy) {
         if (lane == 0)
             *valid = 1;
-        ring_issue<U, SC>(q.c, q.w, slots, lane);
+        ring_issue<U, PATHS>(q.c, q.w, slots, lane);
         q.idx0 += 32 * U;
         if (q.idx0 >= q.c.total) { // on to the warp's next tile
             ++q.j;
@@ -1817,9 +2069,11 @@ template <int U, int PATHS>
 __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned char *smem,
                                                 int warp, int nwarp, int ring_opts) {
     constexpr bool SC = (PATHS & PATH_SCALED) != 0;
-    constexpr int SLOT_BYTES = ring_stage_bytes<U, SC>();
+    constexpr bool CC = (PATHS & PATH_CAST) != 0;
+    constexpr int XR = ring_extra_rows(PATHS);
+    constexpr int SLOT_BYTES = ring_stage_bytes<U, XR>();
     const int lane = threadIdx.x & 31;
-    unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U, SC>();
+    unsigned char *wbase = smem + (size_t)warp * ring_warp_bytes<U, XR>();
     unsigned char *queue = wbase + RING_D * SLOT_BYTES;
     int *valid = reinterpret_cast<int *>(queue + RING_Q * RING_QE);
     const uint32_t slots0 = smem_addr(wbase);
@@ -1856,8 +2110,8 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     }
 #pragma unroll
     for (int st = 0; st < RING_D - 1; ++st)
-        ring_fill<U, SC>(list, q, ord, slots0 + (uint32_t)(st * SLOT_BYTES), queue, queue_s,
-                         valid + st, lane);
+        ring_fill<U, PATHS>(list, q, ord, slots0 + (uint32_t)(st * SLOT_BYTES), queue,
+                            queue_s, valid + st, lane);
     // the storing side: its tile ordinal, walk constants and position
     int js = -1;
     RingTile c;
@@ -1868,8 +2122,8 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
     int sp = 0; // stage to store; the stage before it is filled next
     for (;;) {
         const int sf = sp == 0 ? RING_D - 1 : sp - 1;
-        ring_fill<U, SC>(list, q, ord, slots0 + (uint32_t)(sf * SLOT_BYTES), queue, queue_s,
-                         valid + sf, lane);
+        ring_fill<U, PATHS>(list, q, ord, slots0 + (uint32_t)(sf * SLOT_BYTES), queue,
+                            queue_s, valid + sf, lane);
         cp_async_wait<RING_D - 1>();
         __syncwarp();
         if (!valid[sp]) // stages are filled in order: nothing after this
@@ -1889,6 +2143,8 @@ __device__ __forceinline__ void ring_copy_phase(const PlanList &list, unsigned c
         if (SC && (c.kind & KIND_SCALED))
             ring_store_scaled_dispatch<U, PATHS>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES),
                                                  lane, pp);
+        else if (CC && (c.kind & KIND_CAST))
+            ring_store_cast_dispatch<U>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES), lane);
         else
             ring_store<U>(c, w, slots0 + (uint32_t)(sp * SLOT_BYTES), lane);
         idx0 += 32 * U;

@@ -68,9 +68,10 @@ def _layouts(rng, src, dst, trans, m=257, n=190, P=5, ext_hi=70, mis=(0, 0)):
     return Li, Lf
 
 
-def _check_cast(rng, Li, Lf, src, dst, trans, where=("device", "device")):
+def _check_cast(rng, Li, Lf, src, dst, trans, where=("device", "device"), ai=None):
     import torch
-    ai = _values(rng, Li, src)
+    if ai is None:
+        ai = _values(rng, Li, src)
     af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
     Lt = Li.copy().transpose_or_conjugate(trans) if trans != "N" else Li
     want = _expected(Lt, Lf, ai, af, src, dst, trans)
@@ -147,3 +148,50 @@ def test_cast_argument_checks():
     st = lib.g2g_plan_create_cast(C.byref(dI), capi.FLOAT64, C.byref(dF), capi.FLOAT32,
                                   C.byref(op), None, C.byref(plan))
     assert st == capi.ERROR_UNSUPPORTED
+
+
+def _f64_boundaries(rng, n):
+    """Bit patterns of binary64 values at the binary32 rounding boundaries:
+    exponents around the subnormal, normal and overflow limits, dropped bits
+    at, just below and just above one half ulp (ties to even and odd)."""
+    sign = rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    E = rng.choice(np.r_[0, 1, np.arange(860, 905), np.arange(1140, 1155), 2046, 2047],
+                   n).astype(np.uint64)
+    frac = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    # the bits a binary32 result drops: 29 in the normal range, 926 - E below it
+    sh = np.where((E >= 897) & (E <= 1150), 29, np.clip(926 - E.astype(np.int64), 1, 52))
+    sh = sh.astype(np.uint64)
+    half = np.uint64(1) << (sh - np.uint64(1))
+    low = np.stack([np.zeros(n, np.uint64), half, half - np.uint64(1), half + np.uint64(1),
+                    (np.uint64(1) << sh) - np.uint64(1), frac & ((np.uint64(1) << sh) - np.uint64(1))])
+    pick = low[rng.integers(0, low.shape[0], n), np.arange(n)]
+    frac = (frac & ~((np.uint64(1) << sh) - np.uint64(1))) | pick
+    frac = np.where(rng.random(n) < 0.5, frac ^ (np.uint64(1) << sh), frac)  # odd and even
+    frac &= np.uint64((1 << 52) - 1)
+    return sign | (E << np.uint64(52)) | frac
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("src,dst", [(capi.FLOAT64, capi.FLOAT32), (capi.COMPLEX128, capi.COMPLEX64),
+                                     (capi.FLOAT64, capi.COMPLEX64)])
+def test_cast_rounding_boundaries(src, dst):
+    """Narrowing at every rounding boundary (ties to even, subnormal results,
+    overflow to infinity) against numpy's IEEE conversion, bit for bit."""
+    rng = np.random.default_rng(7 + src + dst)
+    Li, Lf = _layouts(rng, src, dst, "N", m=600, n=300, ext_hi=400)
+    ai = _f64_boundaries(rng, Li.arena_bytes // 8).view(np.uint8).copy()
+    _check_cast(rng, Li, Lf, src, dst, "N", ai=ai)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("src,dst", [(capi.FLOAT32, capi.FLOAT64), (capi.COMPLEX64, capi.COMPLEX128),
+                                     (capi.FLOAT32, capi.COMPLEX128)])
+def test_cast_widening_every_class(src, dst):
+    """Widening of random binary32 bit patterns of every class (zeros,
+    subnormals, normals of every exponent, infinities, NaNs)."""
+    rng = np.random.default_rng(17 + src + dst)
+    Li, Lf = _layouts(rng, src, dst, "N", m=600, n=300, ext_hi=400)
+    u = rng.integers(0, 1 << 32, Li.arena_bytes // 4, dtype=np.uint64).astype(np.uint32)
+    sub = rng.random(len(u)) < 0.2  # a fifth subnormal or zero
+    u[sub] &= np.uint32(0x807FFFFF)
+    _check_cast(rng, Li, Lf, src, dst, "N", ai=u.view(np.uint8).copy())
