@@ -1065,18 +1065,26 @@ g2g_status g2g_plans_execute(int32_t n_plans, g2g_plan *const *plans, void *stre
     }
     cudaStream_t s = (cudaStream_t)stream;
     G2G_CUDA(cudaSetDevice(plans[0]->device));
-    for (int base = 0; base < n_plans; base += g2g::kMaxPlansPerLaunch) {
-        const int n = std::min(n_plans - base, g2g::kMaxPlansPerLaunch);
-        g2g::PlanList l;
-        l.n = 0;
-        l.status = plans[base]->dev.status;
-        for (int k = 0; k < n; ++k) {
-            const g2g_plan *p = plans[base + k];
-            if (p->n_tiles > 0)
-                add_to_list(l, *p);
+    // no kernel instance carries both the cast conversions and the alpha/beta
+    // arithmetic: cast plans launch apart from the others, in order
+    std::vector<g2g_plan *> groups[2];
+    for (int k = 0; k < n_plans; ++k)
+        groups[(plans[k]->paths & 16) ? 1 : 0].push_back(plans[k]);
+    for (const std::vector<g2g_plan *> &grp : groups) {
+        const int m = (int)grp.size();
+        for (int base = 0; base < m; base += g2g::kMaxPlansPerLaunch) {
+            const int n = std::min(m - base, g2g::kMaxPlansPerLaunch);
+            g2g::PlanList l;
+            l.n = 0;
+            l.status = grp[base]->dev.status;
+            for (int k = 0; k < n; ++k) {
+                const g2g_plan *p = grp[base + k];
+                if (p->n_tiles > 0)
+                    add_to_list(l, *p);
+            }
+            if (l.n > 0)
+                G2G_CUDA(g2g::launch_scatter(l, merged_config(grp.data() + base, n), s));
         }
-        if (l.n > 0)
-            G2G_CUDA(g2g::launch_scatter(l, merged_config(plans + base, n), s));
     }
     for (int k = 0; k < n_plans; ++k) {
         G2G_CUDA(cudaEventRecord(plans[k]->done, s));

@@ -195,7 +195,8 @@ g2g_status g2g_plan_execute(g2g_plan *plan, void *stream);
 
 /* Executes several plans as ONE launch of the persistent gather-scatter
  * (the concatenation of their work lists; up to 256 plans per launch, more
- * are split into further launches). Plans must live on one device and their
+ * are split into further launches; cast plans, from g2g_plan_create_cast,
+ * launch apart from the others). Plans must live on one device and their
  * destinations must not overlap. Used for continuous batching of cached
  * plans. */
 g2g_status g2g_plans_execute(int32_t n_plans, g2g_plan *const *plans, void *stream);

@@ -195,3 +195,65 @@ def test_cast_widening_every_class(src, dst):
     sub = rng.random(len(u)) < 0.2  # a fifth subnormal or zero
     u[sub] &= np.uint32(0x807FFFFF)
     _check_cast(rng, Li, Lf, src, dst, "N", ai=u.view(np.uint8).copy())
+
+
+@pytest.mark.gpu
+def test_cast_scaled_and_plain_plans_in_one_multi_plan_launch():
+    """g2g_plans_execute over a cast plan, a scaled plan and a plain plan:
+    the cast plan launches apart (no kernel instance carries both kinds of
+    element arithmetic); every result as when run alone."""
+    import torch
+    rng = np.random.default_rng(77)
+    lib = capi.load()
+    # cast float64 -> float32
+    Lci, Lcf = _layouts(rng, capi.FLOAT64, capi.FLOAT32, "N", m=300, n=200)
+    aci = _values(rng, Lci, capi.FLOAT64)
+    acf = Ls.fill_random(np.zeros(Lcf.arena_bytes, np.uint8), rng)
+    want_c = _expected(Lci, Lcf, aci, acf, capi.FLOAT64, capi.FLOAT32, "N")
+    # scaled float32 and plain complex<double> pairs, checked against the oracle
+    pairs = []
+    for dt, op in [(capi.FLOAT32, ("N", 2.0, 0.5)), (capi.COMPLEX128, ("T", 1.0, 0.0))]:
+        m, n = 250, 180
+        Li = Ls.random_grid_layout(m if op[0] == "N" else n, n if op[0] == "N" else m, 4, dt,
+                                   rng, ext_hi=90)
+        Lf = Ls.random_grid_layout(m, n, 4, dt, rng, ext_hi=90)
+        comp = np.float32 if dt == capi.FLOAT32 else np.float64
+        ai = np.frombuffer(rng.standard_normal(Li.arena_bytes // np.dtype(comp).itemsize)
+                           .astype(comp).tobytes(), np.uint8).copy()
+        af = np.frombuffer(rng.standard_normal(Lf.arena_bytes // np.dtype(comp).itemsize)
+                           .astype(comp).tobytes(), np.uint8).copy()
+        want = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+        pairs.append((Li, Lf, ai, af, op, want))
+    keep, plans, outs = [], [], []
+    dci, dcf = T.to_device([aci, acf])
+    dI, k1 = Lci.desc(dci.data_ptr())
+    dF, k2 = Lcf.desc(dcf.data_ptr())
+    keep += [k1, k2, dI, dF]
+    p = C.c_void_p()
+    capi.check(lib.g2g_plan_create_cast(C.byref(dI), capi.FLOAT64, C.byref(dF), capi.FLOAT32,
+                                        None, None, C.byref(p)))
+    plans.append(p.value)
+    outs.append(dcf)
+    for Li, Lf, ai, af, op, _ in pairs:
+        di, df = T.to_device([ai, af])
+        dI, k1 = Li.desc(di.data_ptr())
+        dF, k2 = Lf.desc(df.data_ptr())
+        o = capi.make_op(*op)
+        keep += [k1, k2, dI, dF, o, di]
+        p = C.c_void_p()
+        capi.check(lib.g2g_plan_create(C.byref(dI), C.byref(dF), Li.dtype, C.byref(o), None,
+                                       C.byref(p)))
+        plans.append(p.value)
+        outs.append(df)
+    s = torch.cuda.Stream()
+    arr = (C.c_void_p * len(plans))(*plans)
+    capi.check(lib.g2g_plans_execute(len(plans), arr, C.c_void_p(s.cuda_stream)))
+    s.synchronize()
+    Lcmp = Ls.Layout(Lcf.rows_split, Lcf.cols_split, Lcf.owners, Lcf.n_ranks, capi.FLOAT32,
+                     [], [], [], [], [], 0)
+    T.assert_arenas_equal(outs[0].cpu().numpy(), want_c, Lcmp, nan_equivalent=True,
+                          what="cast plan in a multi-plan launch")
+    for (Li, Lf, ai, af, op, want), out in zip(pairs, outs[1:]):
+        T.assert_arenas_equal(out.cpu().numpy(), want, Lf, what=f"{op} plan in a multi-plan launch")
+    for p in plans:
+        capi.check(lib.g2g_plan_destroy(C.c_void_p(p)))
