@@ -101,7 +101,8 @@ cudaError_t launch_scatter_512_elem(const PlanList &list, const ScatterConfig &c
 
 
 // Shared memory a transposed tile of edge `tile_dim` with elements of `esz`
-// bytes needs.
+// bytes needs (at least that of a plain transposed tile of 4-byte elements,
+// whose edge is twice `tile_dim`).
 size_t transpose_smem_bytes(int tile_dim, int esz);
 
 // Launches the gather-scatter over the plans of `list`.

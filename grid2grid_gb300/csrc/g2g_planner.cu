@@ -110,8 +110,11 @@ __device__ inline void cell_coords(const PairInfo &p, long long cidx, int nrp, i
 __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
                                   int len_c, int &tr, int &tc) {
     if (kind & KIND_TRANS) {
-        tr = p.tile_dim;
-        tc = p.tile_dim;
+        // plain transposes of 4-byte elements take twice the edge: a tile
+        // then holds as many bytes as one of 16-byte elements
+        const bool wide = !(kind & (KIND_SCALED | KIND_CAST)) && kind_esz(kind) == 4;
+        tr = wide ? 2 * p.tile_dim : p.tile_dim;
+        tc = tr;
     } else {
         int esz = kind_esz(kind);
         tr = len_r < p.tile_rows ? len_r : p.tile_rows;

@@ -45,7 +45,10 @@ cudaError_t kernel_occupancy(const void *fn, int threads, size_t smem, int *occ)
 }
 
 size_t transpose_smem_bytes(int tile_dim, int esz) {
-    return (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;
+    // room for a plain transposed tile of 4-byte elements too (twice the edge)
+    const size_t wide = (size_t)(2 * tile_dim) * (size_t)(2 * tile_dim + 1) * 4u;
+    const size_t own = (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;
+    return own > wide ? own : wide;
 }
 
 int stage_bytes_for(int tile_bytes) {

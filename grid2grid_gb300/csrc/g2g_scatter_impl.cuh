@@ -1038,6 +1038,108 @@ __device__ __forceinline__ void smem_to_global(const Tile &t, int td_shift,
 }
 #undef G2G_MODE_DISPATCH
 
+// Plain transposed tiles of 4-byte elements are twice as wide (edge 2 td,
+// shift tsh = td_shift + 1): four elements per 16-byte register slot, so a
+// thread holds 4 NE of them and a CTA keeps as many bytes in flight as with
+// 16-byte elements. Same views as above: loads along source storage
+// columns, stores along destination columns, 4-byte accesses coalesced over
+// the warp.
+template <int W> __device__ __forceinline__ void slot_set(uint4 &v, uint32_t x) {
+    if (W == 0) v.x = x; else if (W == 1) v.y = x; else if (W == 2) v.z = x; else v.w = x;
+}
+template <int W> __device__ __forceinline__ uint32_t slot_get(const uint4 &v) {
+    return W == 0 ? v.x : (W == 1 ? v.y : (W == 2 ? v.z : v.w));
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void load_slots_w4(const Tile &t, int tsh, uint4 (&v)[NE]) {
+    const int c = threadIdx.x & ((1 << tsh) - 1);
+    const int r0 = threadIdx.x >> tsh;
+    const int rstep = THREADS >> tsh;
+    if (c >= t.cols)
+        return;
+    uint64_t a = t.src + (uint64_t)((long long)r0 * t.src_ld + (long long)c * 4);
+    const uint64_t step = (uint64_t)((long long)rstep * t.src_ld);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            if (r0 + (4 * i + w) * rstep < t.rows) {
+                const uint32_t x = ldg_w<uint32_t>(a);
+                if (w == 0) slot_set<0>(v[i], x);
+                else if (w == 1) slot_set<1>(v[i], x);
+                else if (w == 2) slot_set<2>(v[i], x);
+                else slot_set<3>(v[i], x);
+            }
+            a += step;
+        }
+    }
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void slots_to_smem_w4(const Tile &t, int tsh, const uint4 (&v)[NE],
+                                                 unsigned char *smem) {
+    const int T = 1 << tsh;
+    const int c = threadIdx.x & (T - 1);
+    const int r0 = threadIdx.x >> tsh;
+    const int rstep = THREADS >> tsh;
+    if (c >= t.cols)
+        return;
+    uint32_t *p = reinterpret_cast<uint32_t *>(smem) + r0 * (T + 1) + c;
+    const int step = rstep * (T + 1);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            if (r0 + (4 * i + w) * rstep < t.rows)
+                *p = w == 0 ? slot_get<0>(v[i])
+                            : (w == 1 ? slot_get<1>(v[i]) : (w == 2 ? slot_get<2>(v[i]) : slot_get<3>(v[i])));
+            p += step;
+        }
+    }
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void smem_to_global_w4(const Tile &t, int tsh,
+                                                  const unsigned char *smem) {
+    const int T = 1 << tsh;
+    const int r = threadIdx.x & (T - 1);
+    const int c0 = threadIdx.x >> tsh;
+    const int cstep = THREADS >> tsh;
+    if (r >= t.rows)
+        return;
+    const uint32_t *p = reinterpret_cast<const uint32_t *>(smem) + r * (T + 1) + c0;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 4);
+    const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
+#pragma unroll
+    for (int i = 0; i < 4 * NE; ++i) {
+        if (c0 + i * cstep < t.cols)
+            st_u32(a, p[i * cstep]);
+        a += step;
+    }
+}
+// Plain transposed tiles: the wide form for 4-byte elements.
+template <int THREADS, int NE>
+__device__ __forceinline__ void plain_load_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    if (kind_esz(t.kind) == 4)
+        load_slots_w4<THREADS, NE>(t, td_shift + 1, v);
+    else
+        load_tile_slots<THREADS, NE>(t, td_shift, v);
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void plain_slots_to_smem(const Tile &t, int td_shift,
+                                                    const uint4 (&v)[NE], unsigned char *smem) {
+    if (kind_esz(t.kind) == 4)
+        slots_to_smem_w4<THREADS, NE>(t, td_shift + 1, v, smem);
+    else
+        slots_to_smem<THREADS, NE>(t, td_shift, v, smem);
+}
+template <int THREADS, int NE>
+__device__ __forceinline__ void plain_smem_to_global(const Tile &t, int td_shift,
+                                                     const unsigned char *smem) {
+    if (kind_esz(t.kind) == 4)
+        smem_to_global_w4<THREADS, NE>(t, td_shift + 1, smem);
+    else
+        smem_to_global<THREADS, NE>(t, td_shift, smem);
+}
+
 // ------------------------------------------------- scaled transposed tiles
 // Element words <-> element type.
 template <typename T> __device__ __forceinline__ T from_words(uint4 v);
@@ -1372,7 +1474,7 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     if (ti < n) {
         cur = *locate_cta(list, ti, cur_pairs);
         if (PIPE && is_plain_transpose(cur))
-            load_tile_slots<THREADS, NE>(cur, td_shift, v);
+            plain_load_slots<THREADS, NE>(cur, td_shift, v);
     }
     while (ti < n) {
         const long long next = ti + G;
@@ -1393,23 +1495,31 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
         if ((PATHS & (PATH_TRANSPOSE | PATH_SCALED)) && staged) {
             __syncthreads(); // earlier tiles are out of shared memory
             // transposed tiles, plain or scaled, staged through shared memory
-            if (!PIPE)
-                load_tile_slots<THREADS, NE>(cur, td_shift, v);
-            slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
+            const bool plain = is_plain_transpose(cur);
+            if (!PIPE) {
+                if (plain)
+                    plain_load_slots<THREADS, NE>(cur, td_shift, v);
+                else
+                    load_tile_slots<THREADS, NE>(cur, td_shift, v);
+            }
+            if (plain)
+                plain_slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
+            else
+                slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
             __syncthreads();
             if (PIPE && next < n && is_plain_transpose(nxt))
-                load_tile_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
+                plain_load_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
             if ((PATHS & PATH_SCALED) && (cur.kind & KIND_SCALED))
                 scaled_transpose_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             else
-                smem_to_global<THREADS, NE>(cur, td_shift, smem);
+                plain_smem_to_global<THREADS, NE>(cur, td_shift, smem);
         } else {
             if ((PATHS & PATH_CAST) && (cur.kind & KIND_CAST))
                 cast_dispatch<THREADS>(cur, smem, td);
             else if (PATHS & PATH_SCALED)
                 scaled_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             if (PIPE && next < n && is_plain_transpose(nxt))
-                load_tile_slots<THREADS, NE>(nxt, td_shift, v);
+                plain_load_slots<THREADS, NE>(nxt, td_shift, v);
         }
         if (next < n) {
             cur = nxt;
