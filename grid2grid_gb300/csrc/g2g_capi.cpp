@@ -358,7 +358,8 @@ struct g2g_plan {
     bool any_trans = false;
     int max_trans_esz = 0;
     int paths = 0; // tile paths the work list needs (1 copy, 2 transpose,
-                   // 4 scaled real, 8 scaled complex, 16 cast)
+                   // 4 scaled real, 8 scaled complex, 16 cast, 32 transposes
+                   // of 4- or 8-byte elements)
     bool host_memory = false; // some block lives in pinned host memory
     g2g_tuning tuning;
     // device
@@ -568,8 +569,9 @@ void assemble(g2g_plan &pl) {
         else if (p.scaled) // real and complex arithmetic are separate kernel paths
             pl.paths |= ((p.dtype == G2G_COMPLEX64 || p.dtype == G2G_COMPLEX128) ? 8 : 4) |
                         (warp_elem && any_plain ? 1 : 0);
-        else
-            pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0);
+        else // 32: plain transposes of 4- or 8-byte elements (wide / tall tiles)
+            pl.paths |= (any_plain ? 1 : 0) | (p.any_trans ? 2 : 0) |
+                        (p.any_trans && p.esz <= 8 ? 32 : 0);
     }
 }
 

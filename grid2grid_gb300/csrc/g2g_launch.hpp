@@ -65,7 +65,8 @@ struct ScatterConfig {
     int tile_dim = 32;       // transposed tile edge (16 or 32)
     size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled real,
-                             // 8 scaled complex
+                             // 8 scaled complex, 16 cast, 32 transposes of 4- or
+                             // 8-byte elements
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
     int ring = 0;            // plain copies through the per-warp cp.async ring
     int run_shift = 0;       // ring: runs of 2^run_shift consecutive tiles per warp

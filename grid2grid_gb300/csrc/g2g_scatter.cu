@@ -45,10 +45,13 @@ cudaError_t kernel_occupancy(const void *fn, int threads, size_t smem, int *occ)
 }
 
 size_t transpose_smem_bytes(int tile_dim, int esz) {
-    // room for a plain transposed tile of 4-byte elements too (twice the edge)
+    // room for the plain transposed tiles of 4-byte elements (twice the
+    // edge) and of 8-byte ones (twice the rows) too
     const size_t wide = (size_t)(2 * tile_dim) * (size_t)(2 * tile_dim + 1) * 4u;
+    const size_t tall = (size_t)(2 * tile_dim) * (size_t)(tile_dim + 1) * 8u;
     const size_t own = (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;
-    return own > wide ? own : wide;
+    const size_t m = wide > tall ? wide : tall;
+    return own > m ? own : m;
 }
 
 int stage_bytes_for(int tile_bytes) {
@@ -104,6 +107,8 @@ cudaError_t preload_scatter_kernels() {
     list.n = 1;
     list.total_copy = 1;
     const int path_sets[] = {PATH_COPY, PATH_TRANSPOSE, PATH_COPY | PATH_TRANSPOSE,
+                             PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
+                             PATH_COPY | PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
                              PATH_COPY | PATH_SCALED_REAL, PATH_COPY | PATH_SCALED_COMPLEX,
                              PATH_COPY | PATH_CAST};
     for (int threads : {256, 512})

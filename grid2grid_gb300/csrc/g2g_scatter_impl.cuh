@@ -49,7 +49,9 @@ enum : int {
     PATH_SCALED_REAL = 4,    // scaled float / double tiles
     PATH_SCALED_COMPLEX = 8, // scaled complex tiles (more registers)
     PATH_SCALED = PATH_SCALED_REAL | PATH_SCALED_COMPLEX,
-    PATH_CAST = 16           // tiles converting the element type
+    PATH_CAST = 16,          // tiles converting the element type
+    PATH_NARROW_TRANSPOSE = 32 // plain transposed tiles of 4- or 8-byte elements
+                               // (the wide and tall tile shapes)
 };
 
 // ---------------------------------------------------------------- memory ops
@@ -1115,29 +1117,128 @@ __device__ __forceinline__ void smem_to_global_w4(const Tile &t, int tsh,
         a += step;
     }
 }
-// Plain transposed tiles: the wide form for 4-byte elements.
-template <int THREADS, int NE>
-__device__ __forceinline__ void plain_load_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
-    if (kind_esz(t.kind) == 4)
-        load_slots_w4<THREADS, NE>(t, td_shift + 1, v);
-    else
-        load_tile_slots<THREADS, NE>(t, td_shift, v);
+// Plain transposed tiles of 8-byte elements are twice as tall: 2 td final
+// rows (the destination's contiguous direction: 512-byte runs at td = 32) by
+// td final columns, two elements per register slot. Loads: lanes along the
+// final columns (the source's contiguous direction), lines over the final
+// rows; stores: lanes along the final rows, lines over the final columns.
+// Shared memory [row][col] with a pitch of td + 1 elements keeps both views
+// free of bank conflicts.
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void load_slots_t8(const Tile &t, int csh, uint4 (&v)[NE]) {
+    const int c = threadIdx.x & ((1 << csh) - 1);
+    const int r0 = threadIdx.x >> csh;
+    const int rstep = THREADS >> csh;
+    if (c >= t.cols)
+        return;
+    uint64_t a = t.src + (uint64_t)((long long)r0 * t.src_ld + (long long)c * 8);
+    const uint64_t step = (uint64_t)((long long)rstep * t.src_ld);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (r0 + (2 * i + h) * rstep < t.rows) {
+                const uint4 e = ld_elem_raw(a, MODE);
+                if (h == 0) {
+                    v[i].x = e.x;
+                    v[i].y = e.y;
+                } else {
+                    v[i].z = e.x;
+                    v[i].w = e.y;
+                }
+            }
+            a += step;
+        }
+    }
 }
 template <int THREADS, int NE>
+__device__ __forceinline__ void slots_to_smem_t8(const Tile &t, int csh, const uint4 (&v)[NE],
+                                                 unsigned char *smem) {
+    const int TC = 1 << csh;
+    const int c = threadIdx.x & (TC - 1);
+    const int r0 = threadIdx.x >> csh;
+    const int rstep = THREADS >> csh;
+    if (c >= t.cols)
+        return;
+    uint2 *p = reinterpret_cast<uint2 *>(smem) + r0 * (TC + 1) + c;
+    const int step = rstep * (TC + 1);
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+        if (r0 + (2 * i) * rstep < t.rows)
+            p[0] = make_uint2(v[i].x, v[i].y);
+        if (r0 + (2 * i + 1) * rstep < t.rows)
+            p[step] = make_uint2(v[i].z, v[i].w);
+        p += 2 * step;
+    }
+}
+template <int THREADS, int NE, int MODE>
+__device__ __forceinline__ void smem_to_global_t8(const Tile &t, int csh,
+                                                  const unsigned char *smem) {
+    const int TC = 1 << csh;
+    const int TR = 2 * TC;
+    const int r = threadIdx.x & (TR - 1);
+    const int c0 = threadIdx.x / TR;
+    const int cstep = THREADS / TR;
+    if (r >= t.rows)
+        return;
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    const uint2 *p = reinterpret_cast<const uint2 *>(smem) + r * (TC + 1) + c0;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 8);
+    const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
+#pragma unroll
+    for (int i = 0; i < 2 * NE; ++i) {
+        if (c0 + i * cstep < t.cols) {
+            const uint2 w = p[i * cstep];
+            // complex<float>: the imaginary part's sign is the top word's
+            st_elem_raw(a, make_uint4(w.x, conj ? (w.y ^ 0x80000000u) : w.y, 0u, 0u), MODE);
+        }
+        a += step;
+    }
+}
+
+// Plain transposed tiles: the wide form for 4-byte elements, the tall form
+// for 8-byte ones, the td x td form for 16-byte ones. Kernel instances whose
+// plans hold no narrow transposes (NARROW false) carry the td x td form only,
+// so its register allocation is not shared with the other two.
+template <int THREADS, int NE, bool NARROW>
+__device__ __forceinline__ void plain_load_slots(const Tile &t, int td_shift, uint4 (&v)[NE]) {
+    if constexpr (!NARROW) {
+        load_tile_slots<THREADS, NE>(t, td_shift, v);
+        return;
+    }
+    switch (elem_mode(t)) {
+    case EM_4: load_slots_w4<THREADS, NE>(t, td_shift + 1, v); break;
+    case EM_8: load_slots_t8<THREADS, NE, EM_8>(t, td_shift, v); break;
+    case EM_8_SPLIT: load_slots_t8<THREADS, NE, EM_8_SPLIT>(t, td_shift, v); break;
+    default: load_tile_slots<THREADS, NE>(t, td_shift, v); break;
+    }
+}
+template <int THREADS, int NE, bool NARROW>
 __device__ __forceinline__ void plain_slots_to_smem(const Tile &t, int td_shift,
                                                     const uint4 (&v)[NE], unsigned char *smem) {
-    if (kind_esz(t.kind) == 4)
-        slots_to_smem_w4<THREADS, NE>(t, td_shift + 1, v, smem);
-    else
+    if constexpr (!NARROW) {
         slots_to_smem<THREADS, NE>(t, td_shift, v, smem);
+        return;
+    }
+    switch (kind_esz(t.kind)) {
+    case 4: slots_to_smem_w4<THREADS, NE>(t, td_shift + 1, v, smem); break;
+    case 8: slots_to_smem_t8<THREADS, NE>(t, td_shift, v, smem); break;
+    default: slots_to_smem<THREADS, NE>(t, td_shift, v, smem); break;
+    }
 }
-template <int THREADS, int NE>
+template <int THREADS, int NE, bool NARROW>
 __device__ __forceinline__ void plain_smem_to_global(const Tile &t, int td_shift,
                                                      const unsigned char *smem) {
-    if (kind_esz(t.kind) == 4)
-        smem_to_global_w4<THREADS, NE>(t, td_shift + 1, smem);
-    else
+    if constexpr (!NARROW) {
         smem_to_global<THREADS, NE>(t, td_shift, smem);
+        return;
+    }
+    switch (elem_mode(t)) {
+    case EM_4: smem_to_global_w4<THREADS, NE>(t, td_shift + 1, smem); break;
+    case EM_8: smem_to_global_t8<THREADS, NE, EM_8>(t, td_shift, smem); break;
+    case EM_8_SPLIT: smem_to_global_t8<THREADS, NE, EM_8_SPLIT>(t, td_shift, smem); break;
+    default: smem_to_global<THREADS, NE>(t, td_shift, smem); break;
+    }
 }
 
 // ------------------------------------------------- scaled transposed tiles
@@ -1445,6 +1546,7 @@ __device__ __forceinline__ void scaled_transpose_dispatch(const Tile &t, const P
 template <int U, int THREADS> struct MinBlocks {
     static constexpr int value = (1024 / THREADS) > 0 ? (1024 / THREADS) : 1;
 };
+
 // Kernels with scaled tiles: 128 registers (512 resident threads per SM)
 // for the complex arithmetic (and the element conversions of cast tiles),
 // 80 (768 threads) for the real one, so that neither spills.
@@ -1464,6 +1566,8 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     // time: the next tile's loads held across their element code would cost
     // more registers than the overlap gains.
     constexpr bool PIPE = (PATHS & PATH_TRANSPOSE) && !(PATHS & (PATH_SCALED | PATH_CAST));
+    // kernels with element arithmetic take every plain transposed shape
+    constexpr bool NARROW = (PATHS & (PATH_NARROW_TRANSPOSE | PATH_SCALED | PATH_CAST)) != 0;
     const int td_shift = td >= 32 ? 5 : 4;
     const long long n = list.total_cta;
     const long long G = gridDim.x;
@@ -1474,7 +1578,7 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     if (ti < n) {
         cur = *locate_cta(list, ti, cur_pairs);
         if (PIPE && is_plain_transpose(cur))
-            plain_load_slots<THREADS, NE>(cur, td_shift, v);
+            plain_load_slots<THREADS, NE, NARROW>(cur, td_shift, v);
     }
     while (ti < n) {
         const long long next = ti + G;
@@ -1498,28 +1602,28 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
             const bool plain = is_plain_transpose(cur);
             if (!PIPE) {
                 if (plain)
-                    plain_load_slots<THREADS, NE>(cur, td_shift, v);
+                    plain_load_slots<THREADS, NE, NARROW>(cur, td_shift, v);
                 else
                     load_tile_slots<THREADS, NE>(cur, td_shift, v);
             }
             if (plain)
-                plain_slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
+                plain_slots_to_smem<THREADS, NE, NARROW>(cur, td_shift, v, smem);
             else
                 slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
             __syncthreads();
             if (PIPE && next < n && is_plain_transpose(nxt))
-                plain_load_slots<THREADS, NE>(nxt, td_shift, v); // in flight during the stores
+                plain_load_slots<THREADS, NE, NARROW>(nxt, td_shift, v); // in flight during the stores
             if ((PATHS & PATH_SCALED) && (cur.kind & KIND_SCALED))
                 scaled_transpose_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             else
-                plain_smem_to_global<THREADS, NE>(cur, td_shift, smem);
+                plain_smem_to_global<THREADS, NE, NARROW>(cur, td_shift, smem);
         } else {
             if ((PATHS & PATH_CAST) && (cur.kind & KIND_CAST))
                 cast_dispatch<THREADS>(cur, smem, td);
             else if (PATHS & PATH_SCALED)
                 scaled_dispatch<THREADS, PATHS>(cur, cur_pairs, smem, td);
             if (PIPE && next < n && is_plain_transpose(nxt))
-                plain_load_slots<THREADS, NE>(nxt, td_shift, v);
+                plain_load_slots<THREADS, NE, NARROW>(nxt, td_shift, v);
         }
         if (next < n) {
             cur = nxt;
@@ -2426,9 +2530,12 @@ template <int THREADS>
 cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
     if (cfg.paths == PATH_COPY)
         return launch_u<THREADS, PATH_COPY>(l, cfg, s);
-    if (cfg.paths == PATH_TRANSPOSE)
-        return launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
-    return launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
+    const bool narrow = (cfg.paths & PATH_NARROW_TRANSPOSE) != 0;
+    if ((cfg.paths & ~PATH_NARROW_TRANSPOSE) == PATH_TRANSPOSE)
+        return narrow ? launch_u<THREADS, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)
+                      : launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
+    return narrow ? launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)
+                  : launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
 }
 
 // Plans with element arithmetic: scaled or cast tiles (and any others).
