@@ -396,3 +396,31 @@ def test_tiny_pieces_and_short_tiles(tuning):
     got = T.gpu_run(inits, finals, ias, fas, how="plan", tuning=tuning, executes=2)
     for k in range(len(inits)):
         T.assert_arenas_equal(got[k], want[k], finals[k], what=f"{tuning} pair {k}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dt", [capi.FLOAT32, capi.FLOAT64, capi.COMPLEX64, capi.COMPLEX128])
+@pytest.mark.parametrize("t", ["T", "C"])
+@pytest.mark.parametrize("tile_dim", [16, 32])
+def test_transposed_tile_shapes_match_port(dt, t, tile_dim):
+    """Plain transposes on every tile shape: 4-byte elements on tiles of twice
+    the edge, 8-byte ones on tiles of twice the rows (8-byte aligned and
+    4-byte aligned complex<float>), 16-byte ones on td x td tiles; blocks at
+    4 / 8 bytes past a 16-byte boundary, pieces of every size up to 300."""
+    rng = np.random.default_rng(500 + 10 * dt + tile_dim + (t == "C"))
+    comp = 8 if dt in (capi.FLOAT64, capi.COMPLEX128) else 4
+    inits, finals, ias, fas = [], [], [], []
+    for mis in (0, 4, 8, 12):
+        m, n = int(rng.integers(50, 420)), int(rng.integers(50, 420))
+        mi = (mis - mis % comp)
+        Li = Ls.random_grid_layout(n, m, 5, dt, rng, ext_hi=300, byte_misalign=mi)
+        Lf = Ls.random_grid_layout(m, n, 5, dt, rng, ext_hi=300,
+                                   byte_misalign=(mi + comp) % 16 - ((mi + comp) % 16) % comp)
+        inits.append(Li); finals.append(Lf)
+        ias.append(Ls.fill_random(np.zeros(Li.arena_bytes, np.uint8), rng))
+        fas.append(Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng))
+    ops = [(t, 1.0, 0.0)] * len(inits)
+    want = T.port_run(inits, finals, ias, fas, ops)
+    got = T.gpu_run(inits, finals, ias, fas, ops, how="plan", tuning=dict(tile_dim=tile_dim))
+    for k in range(len(inits)):
+        T.assert_arenas_equal(got[k], want[k], finals[k], what=f"dt{dt} {t} td{tile_dim} pair {k}")
