@@ -110,13 +110,13 @@ __device__ inline void cell_coords(const PairInfo &p, long long cidx, int nrp, i
 __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
                                   int len_c, int &tr, int &tc) {
     if (kind & KIND_TRANS) {
-        // plain transposes of 4-byte elements take twice the edge, those of
-        // 8-byte elements twice the rows: a tile then holds as many bytes as
-        // one of 16-byte elements
-        const bool plain = !(kind & (KIND_SCALED | KIND_CAST));
+        // transposes (plain or scaled) of 4-byte elements take twice the
+        // edge, those of 8-byte elements twice the rows: a tile then holds as
+        // many bytes as one of 16-byte elements
+        const bool shaped = !(kind & KIND_CAST);
         const int esz = kind_esz(kind);
-        tr = plain && esz <= 8 ? 2 * p.tile_dim : p.tile_dim;
-        tc = plain && esz == 4 ? 2 * p.tile_dim : p.tile_dim;
+        tr = shaped && esz <= 8 ? 2 * p.tile_dim : p.tile_dim;
+        tc = shaped && esz == 4 ? 2 * p.tile_dim : p.tile_dim;
     } else {
         int esz = kind_esz(kind);
         tr = len_r < p.tile_rows ? len_r : p.tile_rows;

@@ -1304,32 +1304,35 @@ template <int MODE> __device__ __forceinline__ uint4 ld_dst_elem(uint64_t a) {
     return make_uint4(ld_dst_u32(a), ld_dst_u32(a + 4), ld_dst_u32(a + 8), ld_dst_u32(a + 12));
 }
 
-// smem_to_global_m with beta*d + alpha*e on every element.
-template <int THREADS, int NE, int MODE, typename T>
-__device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int td_shift,
+// smem_to_global_m with beta*d + alpha*e on every element, for a tile of
+// 2^rsh rows by 2^csh columns staged [row][column] with a pitch of
+// 2^csh + 1 elements.
+template <int THREADS, int MODE, typename T>
+__device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int rsh, int csh,
                                                         const unsigned char *smem, T alpha,
                                                         T beta) {
     constexpr int ESZ = ModeEsz<MODE>::value;
     static_assert(ESZ == (int)sizeof(T), "element mode matches the element type");
-    const int td = 1 << td_shift;
-    const int r = threadIdx.x & (td - 1);
-    const int c0 = threadIdx.x >> td_shift;
-    const int cstep = THREADS >> td_shift;
+    const int pitch = (1 << csh) + 1;
+    const int r = threadIdx.x & ((1 << rsh) - 1);
+    const int c0 = threadIdx.x >> rsh;
+    const int cstep = THREADS >> rsh;
+    const int n = ((1 << (rsh + csh)) + THREADS - 1) / THREADS; // elements per thread
     if (r >= t.rows)
         return;
     const bool conj = (t.kind & KIND_CONJ) != 0;
-    const unsigned char *p = smem + (size_t)(r * (td + 1) + c0) * ESZ;
+    const unsigned char *p = smem + (size_t)(r * pitch + c0) * ESZ;
     uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ESZ);
     const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
     // the destination elements are pulled into L1 together (prefetches hold
     // no registers), then combined one at a time: the complex arithmetic of
     // several elements would not fit the register budget
-#pragma unroll
-    for (int i = 0; i < NE; ++i)
+#pragma unroll 1
+    for (int i = 0; i < n; ++i)
         if (c0 + i * cstep < t.cols)
             asm volatile("prefetch.global.L1 [%0];" ::"l"(a + (uint64_t)i * step));
 #pragma unroll 1
-    for (int i = 0; i < NE; ++i) {
+    for (int i = 0; i < n; ++i) {
         if (c0 + i * cstep < t.cols) {
             uint4 e = lds_elem(p, ESZ);
             if (conj) {
@@ -1347,31 +1350,35 @@ __device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int td_sh
 }
 
 // Stores a scaled transposed (+ conjugated) tile already staged in shared
-// memory (by the plain transposed path's loads): beta*d + alpha*op(s).
+// memory (by the transposed path's loads, in the tile shape of its element
+// size: 4-byte 2td x 2td, 8-byte 2td rows x td columns, 16-byte td x td):
+// beta*d + alpha*op(s).
 template <int THREADS, typename T>
 __device__ __forceinline__ void scaled_transpose_store(const Tile &t, const PairInfo *pairs,
                                                        const unsigned char *smem, int td) {
-    constexpr int NE = 1024 / THREADS;
     const int td_shift = td >= 32 ? 5 : 4;
     const T alpha = scalar_from<T>(pairs[t.pair].alpha);
     const T beta = scalar_from<T>(pairs[t.pair].beta);
     const int mode = elem_mode(t);
     if constexpr (sizeof(T) == 4) {
-        smem_to_global_scaled_m<THREADS, NE, EM_4, T>(t, td_shift, smem, alpha, beta);
+        smem_to_global_scaled_m<THREADS, EM_4, T>(t, td_shift + 1, td_shift + 1, smem, alpha,
+                                                  beta);
     } else if constexpr (sizeof(T) == 8) {
         if (mode == EM_8)
-            smem_to_global_scaled_m<THREADS, NE, EM_8, T>(t, td_shift, smem, alpha, beta);
+            smem_to_global_scaled_m<THREADS, EM_8, T>(t, td_shift + 1, td_shift, smem, alpha,
+                                                      beta);
         else
-            smem_to_global_scaled_m<THREADS, NE, EM_8_SPLIT, T>(t, td_shift, smem, alpha, beta);
+            smem_to_global_scaled_m<THREADS, EM_8_SPLIT, T>(t, td_shift + 1, td_shift, smem,
+                                                            alpha, beta);
     } else {
         if (mode == EM_16)
-            smem_to_global_scaled_m<THREADS, NE, EM_16, T>(t, td_shift, smem, alpha, beta);
+            smem_to_global_scaled_m<THREADS, EM_16, T>(t, td_shift, td_shift, smem, alpha, beta);
         else if (mode == EM_16_SPLIT8)
-            smem_to_global_scaled_m<THREADS, NE, EM_16_SPLIT8, T>(t, td_shift, smem, alpha,
-                                                                   beta);
+            smem_to_global_scaled_m<THREADS, EM_16_SPLIT8, T>(t, td_shift, td_shift, smem, alpha,
+                                                              beta);
         else
-            smem_to_global_scaled_m<THREADS, NE, EM_16_SPLIT4, T>(t, td_shift, smem, alpha,
-                                                                   beta);
+            smem_to_global_scaled_m<THREADS, EM_16_SPLIT4, T>(t, td_shift, td_shift, smem, alpha,
+                                                              beta);
     }
 }
 
@@ -1599,17 +1606,11 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
         if ((PATHS & (PATH_TRANSPOSE | PATH_SCALED)) && staged) {
             __syncthreads(); // earlier tiles are out of shared memory
             // transposed tiles, plain or scaled, staged through shared memory
-            const bool plain = is_plain_transpose(cur);
-            if (!PIPE) {
-                if (plain)
-                    plain_load_slots<THREADS, NE, NARROW>(cur, td_shift, v);
-                else
-                    load_tile_slots<THREADS, NE>(cur, td_shift, v);
-            }
-            if (plain)
-                plain_slots_to_smem<THREADS, NE, NARROW>(cur, td_shift, v, smem);
-            else
-                slots_to_smem<THREADS, NE>(cur, td_shift, v, smem);
+            // (transposed tiles of 4- and 8-byte elements, plain or scaled,
+            // come in the wide and tall shapes)
+            if (!PIPE)
+                plain_load_slots<THREADS, NE, NARROW>(cur, td_shift, v);
+            plain_slots_to_smem<THREADS, NE, NARROW>(cur, td_shift, v, smem);
             __syncthreads();
             if (PIPE && next < n && is_plain_transpose(nxt))
                 plain_load_slots<THREADS, NE, NARROW>(nxt, td_shift, v); // in flight during the stores
