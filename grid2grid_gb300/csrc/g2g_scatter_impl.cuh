@@ -1098,6 +1098,34 @@ __device__ __forceinline__ void slots_to_smem_w4(const Tile &t, int tsh, const u
         }
     }
 }
+// Stores of the tall tiles: one warp per destination column, lanes along
+// its rows, every 32-lane pass starting on a 32-byte sector of the
+// destination, so that a pass writes whole sectors except at the column's
+// two ends (a store covering part of a sector that is absent from L2 makes
+// L2 fetch the rest from DRAM): double and complex<float> 'T' on random
+// grids 0.70 -> 0.75 of the copy peak.
+template <int THREADS, int MODE>
+__device__ __forceinline__ void smem_to_global_sect(const Tile &t, int pitch,
+                                                    const unsigned char *smem) {
+    constexpr int ESZ = ModeEsz<MODE>::value;
+    constexpr int NWARP = THREADS / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool conj = (t.kind & KIND_CONJ) != 0;
+    for (int c = warp; c < t.cols; c += NWARP) {
+        const uint64_t dcol = t.dst + (uint64_t)((long long)c * t.dst_ld);
+        const int lead = (int)(dcol & 31u) / ESZ; // elements of the first sector before row 0
+        for (int r = lane - lead; r < t.rows; r += 32) {
+            if (r < 0)
+                continue;
+            uint4 e = lds_elem(smem + (size_t)(r * pitch + c) * ESZ, ESZ);
+            if (ESZ == 8 && conj) // complex<float>: the imaginary sign is the top word's
+                e.y ^= 0x80000000u;
+            st_elem_raw(dcol + (uint64_t)r * ESZ, e, MODE);
+        }
+    }
+}
+// (4-byte elements keep the thread-per-row view: for them the passes'
+// extra index arithmetic costs more issue slots than the fills save.)
 template <int THREADS, int NE>
 __device__ __forceinline__ void smem_to_global_w4(const Tile &t, int tsh,
                                                   const unsigned char *smem) {
@@ -1174,26 +1202,7 @@ __device__ __forceinline__ void slots_to_smem_t8(const Tile &t, int csh, const u
 template <int THREADS, int NE, int MODE>
 __device__ __forceinline__ void smem_to_global_t8(const Tile &t, int csh,
                                                   const unsigned char *smem) {
-    const int TC = 1 << csh;
-    const int TR = 2 * TC;
-    const int r = threadIdx.x & (TR - 1);
-    const int c0 = threadIdx.x / TR;
-    const int cstep = THREADS / TR;
-    if (r >= t.rows)
-        return;
-    const bool conj = (t.kind & KIND_CONJ) != 0;
-    const uint2 *p = reinterpret_cast<const uint2 *>(smem) + r * (TC + 1) + c0;
-    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 8);
-    const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
-#pragma unroll
-    for (int i = 0; i < 2 * NE; ++i) {
-        if (c0 + i * cstep < t.cols) {
-            const uint2 w = p[i * cstep];
-            // complex<float>: the imaginary part's sign is the top word's
-            st_elem_raw(a, make_uint4(w.x, conj ? (w.y ^ 0x80000000u) : w.y, 0u, 0u), MODE);
-        }
-        a += step;
-    }
+    smem_to_global_sect<THREADS, MODE>(t, (1 << csh) + 1, smem);
 }
 
 // Plain transposed tiles: the wide form for 4-byte elements, the tall form
