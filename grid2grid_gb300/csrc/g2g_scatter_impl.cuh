@@ -85,6 +85,14 @@ template <> __device__ __forceinline__ unsigned long long ldg_w<unsigned long lo
     return v;
 }
 template <> __device__ __forceinline__ uint4 ldg_w<uint4>(uint64_t a) { return ldg_v4(a); }
+// A read-only load that allocates in L1 (a sector that the CTA's other
+// warps read too is then fetched once per SM).
+__device__ __forceinline__ uint32_t ldg_l1_u32(uint64_t a) {
+    uint32_t v;
+    asm("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(a));
+    return v;
+}
+
 
 template <typename W> __device__ __forceinline__ void st_w(uint64_t addr, W v);
 template <> __device__ __forceinline__ void st_w<uint32_t>(uint64_t a, uint32_t v) {
@@ -1066,7 +1074,7 @@ __device__ __forceinline__ void load_slots_w4(const Tile &t, int tsh, uint4 (&v)
 #pragma unroll
         for (int w = 0; w < 4; ++w) {
             if (r0 + (4 * i + w) * rstep < t.rows) {
-                const uint32_t x = ldg_w<uint32_t>(a);
+                const uint32_t x = ldg_l1_u32(a);
                 if (w == 0) slot_set<0>(v[i], x);
                 else if (w == 1) slot_set<1>(v[i], x);
                 else if (w == 2) slot_set<2>(v[i], x);
