@@ -1,5 +1,5 @@
 """The C++ interface (grid2grid_gb300/include/grid2grid/*.hpp): the reference's
-types and transform overloads over the C ABI. CPU: the driver in
+types and transform overloads over the C ABI. CPU: the test program in
 tests/cpp/facade_test.cpp compiles against the headers and links the library.
 GPU: it runs -- the reference's four scalapack2scalapack ctest cases and more,
 with virtual ranks as threads calling transform collectively."""
