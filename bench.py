@@ -308,6 +308,12 @@ def run_ours(args):
     t_plan0 = time.perf_counter()
     capi.check(lib.g2g_plan_create_batch(n, dI, dF, dts, ops, sp, C.byref(plan)))
     plan_ms = (time.perf_counter() - t_plan0) * 1e3
+    if args.tuning:  # explicit kernel knobs, e.g. to profile one variant
+        t = capi.Tuning()
+        for kv in args.tuning.split(","):
+            k, v = kv.split("=")
+            setattr(t, k.strip(), int(v))
+        capi.check(lib.g2g_plan_set_tuning(plan, C.byref(t)))
     tuned = None
     if args.autotune:
         t = capi.Tuning()
@@ -843,6 +849,9 @@ def main(argv=None):
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-reps", type=int, default=2)
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--tuning", default="", metavar="K=V,...",
+                    help="g2g_tuning fields for the main plan (e.g. stages=3 for the "
+                         "TMA-staged kernel)")
     ap.add_argument("--alpha-beta", type=lambda v: tuple(float(x) for x in v.split(",")),
                     default=None, metavar="A,B",
                     help="time final = B*final + A*op(initial) on the workload instead "
