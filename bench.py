@@ -391,10 +391,11 @@ def run_ours(args):
     capi.check(lib.g2g_plan_destroy(plan))
 
     # the scaled form on the same layouts: final = 0.5*final + 2*initial
-    scaled = cast = None
+    scaled = cast = gemr2d = None
     if args.batch and rank == 0 and w.ops is None:
         scaled = run_scaled(lib, w, dI, dF, dts, stream, peak, args.steps // 4 or 1)
         cast = run_cast(lib, dev, stream, peak, args.steps // 4 or 1)
+        gemr2d = run_gemr2d(lib, dev, 50)
 
     batched = serving = None
     if args.batch and rank == 0:
@@ -423,7 +424,7 @@ def run_ours(args):
             "data": "synthetic (seeded random bit patterns, device-resident)",
             "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
-            "batched_stream": batched, "serving": serving, "scaled": scaled, "cast": cast,
+            "batched_stream": batched, "serving": serving, "scaled": scaled, "cast": cast, "gemr2d": gemr2d,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
                      "tuning": {k: getattr(info.tuning, k) for k in
@@ -527,6 +528,47 @@ def run_cast(lib, dev, stream, peak, steps, m=16384):
                      "roofline_frac": round(info.bytes_min_traffic / (ms * 1e-3) / 1e9 / peak, 4)}
     del a32, a64
     return out
+
+
+def run_gemr2d(lib, dev, steps, m=4096):
+    """The ScaLAPACK-descriptor front end as a caller of p?gemr2d uses it:
+    one blocking g2g_gemr2d per step on the block-cyclic double configuration
+    (m x m, 32 x 32 blocks -> 128 x 64 blocks on a 2 x 2 grid, lld = local
+    rows), per-rank arrays on the device. The call builds both layouts from
+    the descriptors, finds the cached plan, launches and synchronises."""
+    import torch
+    from grid2grid_gb300 import capi
+
+    def desc(mb, nb):
+        d = capi.ScalapackDesc()
+        d.m, d.n, d.mb, d.nb = m, m, mb, nb
+        d.rsrc = d.csrc = 0
+        d.nprow, d.npcol, d.row_major = 2, 2, 0
+        return d
+    loc = m // 2  # local rows and columns of every rank (m a multiple of 256)
+    a = [torch.randn(loc * loc, dtype=torch.float64, device=dev) for _ in range(4)]
+    b = [torch.zeros(loc * loc, dtype=torch.float64, device=dev) for _ in range(4)]
+    pa = (C.c_void_p * 4)(*[t.data_ptr() for t in a])
+    pb = (C.c_void_p * 4)(*[t.data_ptr() for t in b])
+    lld = (C.c_int32 * 4)(*([loc] * 4))
+    da, db = desc(32, 32), desc(128, 64)
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def call():
+        capi.check(lib.g2g_gemr2d(m, m, pa, 1, 1, C.byref(da), lld, pb, 1, 1, C.byref(db), lld,
+                                  capi.FLOAT64, None, sp))
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / steps
+    return {"call": "g2g_gemr2d (blocking)", "config": f"double {m}^2, 32x32 -> 128x64 on 2x2",
+            "ms_per_call": round(t * 1e3, 4), "value": round(m * m * 8 / t / 1e9, 2),
+            "unit": UNIT, "calls": steps}
 
 
 def run_cast_only(args):

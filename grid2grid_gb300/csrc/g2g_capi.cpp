@@ -22,6 +22,7 @@
 #include <cstring>
 #include <list>
 #include <map>
+#include <functional>
 #include <mutex>
 #include <unordered_map>
 #include <string>
@@ -920,15 +921,19 @@ g2g::Sig one_shot_sig(int n, const g2g_layout_desc *init, const g2g_layout_desc 
     return sig;
 }
 
-// plan (cached) + execute + wait: the reference's blocking transform call
-g2g_status one_shot(int n, const g2g_layout_desc *init, const g2g_layout_desc *fin,
-                    const g2g_dtype *dtypes, g2g_dtype dtype, const g2g_op *ops,
-                    void *stream) {
-    const bool cached = g_cache.cap() > 0 && n >= 1 && init && fin;
+} // namespace
+
+namespace g2g {
+
+// plan (cached under `key`, planned by `make` on a miss; no caching when key
+// is null or the cache is off) + execute + wait
+g2g_status cached_one_shot(const Sig *key, const std::function<g2g_status(g2g_plan **)> &make,
+                           void *stream) {
+    const bool cached = key && g_cache.cap() > 0;
     g2g_plan *plan = nullptr;
-    g2g::Sig sig;
+    Sig sig;
     if (cached) {
-        sig = one_shot_sig(n, init, fin, dtypes, dtype, ops);
+        sig = *key;
         std::lock_guard<std::mutex> lk(g_cache.mu);
         auto it = g_cache.map.find(sig);
         if (it != g_cache.map.end()) {
@@ -940,7 +945,7 @@ g2g_status one_shot(int n, const g2g_layout_desc *init, const g2g_layout_desc *f
         }
     }
     if (!plan) {
-        g2g_status st = create_plan(n, init, fin, dtypes, dtype, ops, &plan);
+        g2g_status st = make(&plan);
         if (st != G2G_SUCCESS)
             return st;
         if (cached) {
@@ -990,6 +995,24 @@ g2g_status one_shot(int n, const g2g_layout_desc *init, const g2g_layout_desc *f
     }
     g2g_status st2 = g2g_plan_destroy(plan);
     return st != G2G_SUCCESS ? st : st2;
+}
+
+} // namespace g2g
+
+namespace {
+
+// the reference's blocking transform call: plan cached under the layouts'
+// signature
+g2g_status one_shot(int n, const g2g_layout_desc *init, const g2g_layout_desc *fin,
+                    const g2g_dtype *dtypes, g2g_dtype dtype, const g2g_op *ops,
+                    void *stream) {
+    g2g::Sig sig;
+    const bool keyed = n >= 1 && init && fin && g_cache.cap() > 0;
+    if (keyed)
+        sig = one_shot_sig(n, init, fin, dtypes, dtype, ops);
+    return g2g::cached_one_shot(
+        keyed ? &sig : nullptr,
+        [&](g2g_plan **p) { return create_plan(n, init, fin, dtypes, dtype, ops, p); }, stream);
 }
 
 } // namespace

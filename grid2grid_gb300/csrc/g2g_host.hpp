@@ -6,6 +6,7 @@
 #include "g2g_launch.hpp"
 
 #include <cstdint>
+#include <functional>
 #include <cstddef>
 #include <vector>
 
@@ -82,5 +83,11 @@ inline void add_layout(Sig &s, const g2g_layout_desc *d) {
     if (d->blocks && d->n_blocks > 0)
         s.add(d->blocks, sizeof(g2g_block_desc) * (size_t)d->n_blocks);
 }
+
+// Plans (through `make` on a miss) or finds in the one-shot plan cache the
+// plan stored under `key` (null: no caching), executes it on `stream` and
+// waits: the blocking calls' common path.
+g2g_status cached_one_shot(const Sig *key, const std::function<g2g_status(g2g_plan **)> &make,
+                           void *stream);
 
 } // namespace g2g

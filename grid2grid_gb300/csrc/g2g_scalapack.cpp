@@ -7,6 +7,7 @@
 
 #include <cstring>
 #include <new>
+#include <utility>
 #include <vector>
 
 struct g2g_layout {
@@ -152,6 +153,43 @@ g2g_status build(const g2g_scalapack_desc *d, int32_t ia, int32_t ja, int32_t m,
     return G2G_SUCCESS;
 }
 
+// Every argument of a gemr2d call that its plan depends on.
+g2g::Sig gemr2d_key(int32_t m, int32_t n, void *const *a_data, int32_t ia, int32_t ja,
+                    const g2g_scalapack_desc *da, const int32_t *lld_a, void *const *b_data,
+                    int32_t ib, int32_t jb, const g2g_scalapack_desc *db, const int32_t *lld_b,
+                    g2g_dtype dtype, const g2g_op *op) {
+    g2g::Sig k;
+    k.add((uint32_t)0x67656d72u); // a tag apart from the layout signatures
+    const int32_t v[] = {m, n, ia, ja, ib, jb, (int32_t)dtype};
+    k.add(v);
+    for (const auto &side : {std::make_pair(da, std::make_pair(a_data, lld_a)),
+                             std::make_pair(db, std::make_pair(b_data, lld_b))}) {
+        const g2g_scalapack_desc *d = side.first;
+        const int32_t f[] = {d->m, d->n, d->mb, d->nb, d->rsrc, d->csrc,
+                             d->nprow, d->npcol, d->row_major};
+        k.add(f);
+        const size_t P = (size_t)d->nprow * (size_t)d->npcol;
+        k.add(side.second.first, P * sizeof(void *));
+        if (side.second.second)
+            k.add(side.second.second, P * sizeof(int32_t));
+        else
+            k.add((int32_t)-1);
+    }
+    g2g_op o;
+    std::memset(&o, 0, sizeof(o));
+    o.trans = 'N';
+    o.alpha[0] = 1.0;
+    if (op) {
+        o.trans = op->trans;
+        std::memcpy(o.alpha, op->alpha, sizeof(o.alpha));
+        std::memcpy(o.beta, op->beta, sizeof(o.beta));
+    }
+    k.add(o.trans);
+    k.add(o.alpha);
+    k.add(o.beta);
+    return k;
+}
+
 } // namespace
 
 extern "C" {
@@ -200,17 +238,30 @@ g2g_status g2g_gemr2d(int32_t m, int32_t n, void *const *a_data, int32_t ia, int
     G2G_TRY(check_desc(desc_b, "gemr2d B"));
     if (m == 0 || n == 0)
         return G2G_SUCCESS;
-    g2g_layout A, B;
-    G2G_TRY(build(desc_a, ia, ja, trans ? n : m, trans ? m : n, a_data, lld_a, dtype, A,
-                  "gemr2d A"));
-    G2G_TRY(build(desc_b, ib, jb, m, n, b_data, lld_b, dtype, B, "gemr2d B"));
-    if (A.desc.n_ranks != B.desc.n_ranks) {
-        // one set of virtual ranks: the smaller grid's ranks are a prefix
-        const int32_t P = A.desc.n_ranks > B.desc.n_ranks ? A.desc.n_ranks : B.desc.n_ranks;
-        A.desc.n_ranks = P;
-        B.desc.n_ranks = P;
-    }
-    return g2g_transform(&A.desc, &B.desc, dtype, op, stream);
+    if (!a_data || !b_data)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "gemr2d: rank data array is NULL");
+    // The call's own arguments key the plan cache, so a repeated call (an
+    // iterative caller's usual pattern) skips building both block lists
+    // (p x q blocks each) and hashing them.
+    const g2g::Sig key = gemr2d_key(m, n, a_data, ia, ja, desc_a, lld_a, b_data, ib, jb, desc_b,
+                                    lld_b, dtype, op);
+    return g2g::cached_one_shot(
+        &key,
+        [&](g2g_plan **plan) {
+            g2g_layout A, B;
+            G2G_TRY(build(desc_a, ia, ja, trans ? n : m, trans ? m : n, a_data, lld_a, dtype, A,
+                          "gemr2d A"));
+            G2G_TRY(build(desc_b, ib, jb, m, n, b_data, lld_b, dtype, B, "gemr2d B"));
+            if (A.desc.n_ranks != B.desc.n_ranks) {
+                // one set of virtual ranks: the smaller grid's ranks are a prefix
+                const int32_t P =
+                    A.desc.n_ranks > B.desc.n_ranks ? A.desc.n_ranks : B.desc.n_ranks;
+                A.desc.n_ranks = P;
+                B.desc.n_ranks = P;
+            }
+            return g2g_plan_create(&A.desc, &B.desc, dtype, op, nullptr, plan);
+        },
+        stream);
 }
 
 } // extern "C"
