@@ -6,7 +6,7 @@
 // once and its destination written once, straight from the initial owner's
 // strided block into the final owner's strided block.
 //
-// Three tile paths (uniform per tile, so no divergence):
+// Four tile paths (uniform per tile, so no divergence):
 //  * plain copies    non-transposed: byte movement in 16-byte chunks aligned
 //                    to the DESTINATION, the chunks of a tile's columns walked
 //                    as one flat sequence by the lanes of a warp. When source
@@ -22,12 +22,19 @@
 //                    shared memory with a padded pitch, loaded coalesced along
 //                    the source's storage columns and stored coalesced along
 //                    the destination's columns, the next tile's loads issued
-//                    before the current one is stored (memory_utils.hpp:124-184).
+//                    before the current one is stored (memory_utils.hpp:124-184);
+//                    td x td for 16-byte elements, 2td x 2td for 4-byte,
+//                    2td x td for 8-byte ones (the same bytes per tile).
 //  * scaled tiles    dst = beta*dst + alpha*op(src) in the element type with
 //                    the rounding of the reference's host arithmetic: every
 //                    product and sum rounded separately, complex products in
 //                    the C99 Annex G form that GCC's std::complex multiply uses
-//                    (memory_utils.hpp:25-39,79-122,186-256).
+//                    (memory_utils.hpp:25-39,79-122,186-256). Non-transposed
+//                    ones ride the copy ring with their destination chunks.
+//  * cast tiles      dst = convert(op(src)) between float / double / complex
+//                    types (no counterpart in the reference); non-transposed
+//                    ones ride the copy ring, up to three source blocks per
+//                    destination chunk.
 #pragma once
 
 #include "g2g_internal.hpp"
@@ -1581,8 +1588,9 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
                                       : MinBlocks<U, THREADS>::value;
 };
 
-// CTA-level tiles (transposed, scaled) of a launch, static striding, with the
-// next transposed tile's loads issued before the current tile is stored.
+// CTA-level tiles (transposed, and scaled or cast ones that are not
+// warp-level) of a launch, static striding, with the next plain transposed
+// tile's loads issued before the current tile is stored.
 template <int THREADS, int PATHS>
 __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
     constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
@@ -1652,7 +1660,8 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
 }
 
 // A warp-level work item on the register path: a plain copy, or (kernels
-// with scaled tiles) a non-transposed scaled tile, by NWARP warps.
+// with scaled or cast tiles) a non-transposed scaled or cast tile, by NWARP
+// warps.
 template <int NWARP, typename S>
 __device__ __forceinline__ void cast_cols_to(const Tile &t, int warp) {
     switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
@@ -2408,8 +2417,8 @@ __global__ void __launch_bounds__(THREADS, (RingMinBlocks<THREADS, PATHS>::value
 
 // The staged variant: a ring of S shared-memory stages filled by TMA bulk
 // copies (see issue_stage / consume_stage); tiles that are not eligible for
-// staging (short columns, transposed, scaled) run on the direct paths in the
-// same loop. Every wait is bounded: on expiry the CTA records the error in
+// staging (short columns, scaled, cast) run on the register path in the same
+// loop, CTA-level tiles after it. Every wait is bounded: on expiry the CTA records the error in
 // *status, waits (bounded) for its other stages and returns.
 constexpr uint64_t STAGE_WAIT_LIMIT_NS = 2000000000ull; // 2 s
 
