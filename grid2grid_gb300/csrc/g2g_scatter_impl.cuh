@@ -1659,9 +1659,7 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     }
 }
 
-// A warp-level work item on the register path: a plain copy, or (kernels
-// with scaled or cast tiles) a non-transposed scaled or cast tile, by NWARP
-// warps.
+// A non-transposed cast tile from source type S on the register path.
 template <int NWARP, typename S>
 __device__ __forceinline__ void cast_cols_to(const Tile &t, int warp) {
     switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
@@ -1678,6 +1676,9 @@ __device__ __forceinline__ void cast_cols_to(const Tile &t, int warp) {
     }
 }
 
+// A warp-level work item on the register path: a plain copy, or (kernels
+// with scaled or cast tiles) a non-transposed scaled or cast tile, by NWARP
+// warps.
 template <int NWARP, int U, int PATHS>
 __device__ __forceinline__ void warp_tile(const Tile &t, int warp, const PairInfo *pairs) {
     if constexpr ((PATHS & PATH_CAST) != 0) {
