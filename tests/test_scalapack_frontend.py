@@ -165,3 +165,11 @@ def test_gemr2d_argument_checks_need_no_device():
                           None, capi.FLOAT64, None, None) == capi.ERROR_INVALID_ARGUMENT
     assert lib.g2g_gemr2d(5, 5, data, 7, 1, C.byref(d), None, data, 1, 1, C.byref(d), None,
                           capi.FLOAT64, None, None) == capi.ERROR_INVALID_ARGUMENT
+    # a missing rank array is refused before the plan cache is consulted
+    assert lib.g2g_gemr2d(5, 5, None, 1, 1, C.byref(d), None, data, 1, 1, C.byref(d), None,
+                          capi.FLOAT64, None, None) == capi.ERROR_INVALID_ARGUMENT
+    assert b"NULL" in lib.g2g_last_error_string()
+    # a request that fails validation is not cached: the same call fails again
+    for _ in range(2):
+        assert lib.g2g_gemr2d(5, 5, data, 7, 1, C.byref(d), None, data, 1, 1, C.byref(d),
+                              None, capi.FLOAT64, None, None) == capi.ERROR_INVALID_ARGUMENT
