@@ -115,3 +115,33 @@ def test_port_matches_reference_live(seed):
         oracle.ref_transform([Li], [Lf], [ai.copy()], [ref_f],
                              [capi.make_op(*ops[0])], oracle.MODE_SINGLE_SCALED)
         T.assert_arenas_equal(got, ref_f, Lf, what=f"dt{dt} {t}")
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference oracle not built here")
+@pytest.mark.parametrize("seed", range(4))
+def test_port_scaled_matches_reference_live(seed):
+    """final = beta*final + alpha*op(initial) on finite values: the port and
+    the live reference agree bit for bit on fresh layouts, every dtype and op."""
+    rng = np.random.default_rng(2000 + seed)
+    for dt in (capi.FLOAT32, capi.FLOAT64, capi.COMPLEX64, capi.COMPLEX128):
+        cplx = dt in (capi.COMPLEX64, capi.COMPLEX128)
+        comp = np.float32 if dt in (capi.FLOAT32, capi.COMPLEX64) else np.float64
+        m, n = int(rng.integers(1, 150)), int(rng.integers(1, 150))
+        P = int(rng.integers(1, 7))
+        t = "NTC"[(seed + dt) % 3]
+        Li = Ls.random_grid_layout(m if t == "N" else n, n if t == "N" else m, P, dt, rng,
+                                   ext_hi=40)
+        Lf = Ls.random_grid_layout(m, n, P, dt, rng, ext_hi=40)
+        w = np.dtype(comp).itemsize
+        ai = np.frombuffer(rng.standard_normal(Li.arena_bytes // w).astype(comp).tobytes(),
+                           np.uint8).copy()
+        af = np.frombuffer(rng.standard_normal(Lf.arena_bytes // w).astype(comp).tobytes(),
+                           np.uint8).copy()
+        a = complex(rng.standard_normal(), rng.standard_normal()) if cplx else float(rng.standard_normal())
+        b = complex(rng.standard_normal(), rng.standard_normal()) if cplx else float(rng.standard_normal())
+        ops = [(t, a, b)]
+        got = T.port_run([Li], [Lf], [ai], [af], ops)[0]
+        ref_f = af.copy()
+        oracle.ref_transform([Li], [Lf], [ai.copy()], [ref_f],
+                             [capi.make_op(*ops[0])], oracle.MODE_SINGLE_SCALED)
+        T.assert_arenas_equal(got, ref_f, Lf, what=f"scaled dt{dt} {t} {a} {b}")
