@@ -37,6 +37,23 @@ def test_exports_every_header_symbol(lib):
     assert set(names) == bound, set(names) ^ bound
 
 
+@pytest.mark.parametrize("lang,std", [("c", "c99"), ("c", "c11"), ("c++", "c++11")])
+def test_header_is_plain_c(tmp_path, lang, std):
+    """The boundary header compiles on its own as strict C and as C++: plain
+    structs, pointers and sizes, no CUDA or C++ types in the signatures."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / ("h.c" if lang == "c" else "h.cpp")
+    src.write_text('#include "grid2grid_gb300.h"\nint main(void) { return 0; }\n')
+    r = subprocess.run([cc, f"-std={std}", "-pedantic", "-Wall", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_version_and_error_string(lib):
     assert b"sm_103a" in lib.g2g_version_string()
     assert isinstance(lib.g2g_last_error_string(), bytes)
