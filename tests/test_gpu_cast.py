@@ -257,3 +257,39 @@ def test_cast_scaled_and_plain_plans_in_one_multi_plan_launch():
         T.assert_arenas_equal(out.cpu().numpy(), want, Lf, what=f"{op} plan in a multi-plan launch")
     for p in plans:
         capi.check(lib.g2g_plan_destroy(C.c_void_p(p)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tuning", [dict(unroll=1), dict(unroll=2), dict(ring=-1),
+                                    dict(stages=2, threads=256), dict(threads=512, unroll=2),
+                                    dict(tile_bytes=2048, l2_prefetch=1)])
+def test_cast_tunings_give_identical_results(tuning):
+    """The cast on every kernel form a tuning selects: the copy ring at each
+    unroll, the register path, the TMA-staged kernel (cast tiles beside it on
+    the register path)."""
+    import torch
+    rng = np.random.default_rng(808)
+    lib = capi.load()
+    for src, dst in [(capi.FLOAT32, capi.FLOAT64), (capi.COMPLEX128, capi.COMPLEX64),
+                     (capi.FLOAT64, capi.COMPLEX128)]:
+        Li, Lf = _layouts(rng, src, dst, "N", m=700, n=400, ext_hi=500, mis=(4, 8))
+        ai = _values(rng, Li, src)
+        af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
+        want = _expected(Li, Lf, ai, af, src, dst, "N")
+        di, df = T.to_device([ai, af])
+        dI, k1 = Li.desc(di.data_ptr())
+        dF, k2 = Lf.desc(df.data_ptr())
+        plan = C.c_void_p()
+        capi.check(lib.g2g_plan_create_cast(C.byref(dI), src, C.byref(dF), dst, None, None,
+                                            C.byref(plan)))
+        t = capi.Tuning()
+        for k, v in tuning.items():
+            setattr(t, k, v)
+        capi.check(lib.g2g_plan_set_tuning(plan, C.byref(t)))
+        capi.check(lib.g2g_plan_execute(plan, None))
+        torch.cuda.synchronize()
+        capi.check(lib.g2g_plan_destroy(plan))
+        Lcmp = Ls.Layout(Lf.rows_split, Lf.cols_split, Lf.owners, Lf.n_ranks,
+                         capi.FLOAT64 if _comp(dst) == 8 else capi.FLOAT32, [], [], [], [], [], 0)
+        T.assert_arenas_equal(df.cpu().numpy(), want, Lcmp, nan_equivalent=True,
+                              what=f"cast {src}->{dst} {tuning}")
