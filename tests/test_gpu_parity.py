@@ -401,13 +401,13 @@ def test_tiny_pieces_and_short_tiles(tuning):
 @pytest.mark.gpu
 @pytest.mark.parametrize("dt", [capi.FLOAT32, capi.FLOAT64, capi.COMPLEX64, capi.COMPLEX128])
 @pytest.mark.parametrize("t", ["T", "C"])
-@pytest.mark.parametrize("tile_dim", [16, 32])
-def test_transposed_tile_shapes_match_port(dt, t, tile_dim):
+@pytest.mark.parametrize("tile_dim,threads", [(16, 256), (32, 256), (32, 512)])
+def test_transposed_tile_shapes_match_port(dt, t, tile_dim, threads):
     """Plain transposes on every tile shape: 4-byte elements on tiles of twice
     the edge, 8-byte ones on tiles of twice the rows (8-byte aligned and
     4-byte aligned complex<float>), 16-byte ones on td x td tiles; blocks at
     4 / 8 bytes past a 16-byte boundary, pieces of every size up to 300."""
-    rng = np.random.default_rng(500 + 10 * dt + tile_dim + (t == "C"))
+    rng = np.random.default_rng(500 + 10 * dt + tile_dim + threads + (t == "C"))
     comp = 8 if dt in (capi.FLOAT64, capi.COMPLEX128) else 4
     inits, finals, ias, fas = [], [], [], []
     for mis in (0, 4, 8, 12):
@@ -421,6 +421,7 @@ def test_transposed_tile_shapes_match_port(dt, t, tile_dim):
         fas.append(Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng))
     ops = [(t, 1.0, 0.0)] * len(inits)
     want = T.port_run(inits, finals, ias, fas, ops)
-    got = T.gpu_run(inits, finals, ias, fas, ops, how="plan", tuning=dict(tile_dim=tile_dim))
+    got = T.gpu_run(inits, finals, ias, fas, ops, how="plan",
+                    tuning=dict(tile_dim=tile_dim, threads=threads))
     for k in range(len(inits)):
         T.assert_arenas_equal(got[k], want[k], finals[k], what=f"dt{dt} {t} td{tile_dim} pair {k}")
