@@ -391,11 +391,20 @@ def run_ours(args):
     capi.check(lib.g2g_plan_destroy(plan))
 
     # the scaled form on the same layouts: final = 0.5*final + 2*initial
-    scaled = cast = gemr2d = None
+    scaled = cast = gemr2d = configs = None
     if args.batch and rank == 0 and w.ops is None:
         scaled = run_scaled(lib, w, dI, dF, dts, stream, peak, args.steps // 4 or 1)
         cast = run_cast(lib, dev, stream, peak, args.steps // 4 or 1)
         gemr2d = run_gemr2d(lib, dev, 50)
+    if args.batch and rank == 0:
+        # the other single-transform configurations, each with its own
+        # roofline: block-cyclic double 4096^2 (L2 flushed before every step)
+        # and the transposed complex<double> 8192^2
+        configs = {}
+        for name in ("block_cyclic_f64_4096", "transposed_c128_8192"):
+            if name != w.name:
+                configs[name] = run_config_leg(lib, name, dev, stream, peak,
+                                               max(args.steps, 20))
 
     batched = serving = None
     if args.batch and rank == 0:
@@ -424,7 +433,8 @@ def run_ours(args):
             "data": "synthetic (seeded random bit patterns, device-resident)",
             "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
-            "batched_stream": batched, "serving": serving, "scaled": scaled, "cast": cast, "gemr2d": gemr2d,
+            "configs": configs, "batched_stream": batched, "serving": serving,
+            "scaled": scaled, "cast": cast, "gemr2d": gemr2d,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
                      "tuning": {k: getattr(info.tuning, k) for k in
@@ -472,6 +482,62 @@ def _time_steps(stream, fn, steps, warmup):
         b.record(stream)
     stream.synchronize()
     return a.elapsed_time(b) / steps
+
+
+def run_config_leg(lib, name, dev, stream, peak, steps):
+    """One single-transform configuration, device-resident, plan cached, one
+    launch per step timed with CUDA events on the launching stream. Inputs
+    smaller than L2 get it flushed before every step, outside the events (a
+    512 MiB write, then a 256 MiB read of another buffer). Achieved traffic =
+    2 * m * n * sizeof(T) per launch over the mean launch time; `traffic` is
+    the DRAM bytes per launch of the committed ncu summary of that kernel."""
+    import torch
+    from grid2grid_gb300 import capi
+    from grid2grid_gb300 import workloads as W
+    w = W.BY_NAME[name]()
+    di, df = _device_arenas(w, dev, 4321)
+    keep = []
+    n = len(w.inits)
+    dI, dF = _desc_array(w.inits, di, keep), _desc_array(w.finals, df, keep)
+    dts = (C.c_int * n)(*w.dtypes())
+    ops = None if w.ops is None else (capi.Op * n)(*[capi.make_op(*o) for o in w.ops])
+    sp = C.c_void_p(stream.cuda_stream)
+    plan = C.c_void_p()
+    capi.check(lib.g2g_plan_create_batch(n, dI, dF, dts, ops, sp, C.byref(plan)))
+    info = capi.PlanInfo()
+    capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
+    flush = flush_rd = None
+    small = w.bytes_moved < 512 * 2**20
+    if small:
+        flush = torch.empty(512 * 2**20, dtype=torch.uint8, device=dev)
+        flush_rd = torch.ones(32 * 2**20, dtype=torch.int64, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for _ in range(5):
+            capi.check(lib.g2g_plan_execute(plan, sp))
+        for k in range(steps):
+            if small:
+                flush.zero_()
+                flush_rd.sum()
+            ev[k][0].record(stream)
+            capi.check(lib.g2g_plan_execute(plan, sp))
+            ev[k][1].record(stream)
+    stream.synchronize()
+    capi.check(lib.g2g_plan_destroy(plan))
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    achieved = info.bytes_min_traffic / (ms * 1e-3) / 1e9
+    del di, df, flush, flush_rd
+    torch.cuda.empty_cache()
+    return {"workload": name, "config": dict(w.meta), "ms_per_step": round(ms, 5),
+            "value": round(w.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
+            "steps": steps, "pieces": info.n_pieces, "tiles": info.n_tiles,
+            "l2": "flushed before every step (outside the events)" if small
+                  else "inputs larger than L2 (no flush)",
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": _profile_traffic("g2g_scatter", name),
+                         "algorithmic_bytes_per_launch": info.bytes_min_traffic}}
 
 
 def run_scaled(lib, w, dI, dF, dts, stream, peak, steps):
@@ -566,7 +632,10 @@ def run_gemr2d(lib, dev, steps, m=4096):
         call()
     torch.cuda.synchronize()
     t = (time.perf_counter() - t0) / steps
-    return {"call": "g2g_gemr2d (blocking)", "config": f"double {m}^2, 32x32 -> 128x64 on 2x2",
+    return {"call": "g2g_gemr2d (blocking call latency: descriptors -> cached plan -> launch "
+                    "-> synchronise; the 128 MiB working set stays in L2 between calls, so "
+                    "this is not an HBM figure -- configs.block_cyclic_f64_4096 is)",
+            "config": f"double {m}^2, 32x32 -> 128x64 on 2x2",
             "ms_per_call": round(t * 1e3, 4), "value": round(m * m * 8 / t / 1e9, 2),
             "unit": UNIT, "calls": steps}
 
@@ -605,6 +674,9 @@ def run_batched(lib, dev, stream, steps, peak):
     t0 = time.perf_counter()
     capi.check(lib.g2g_plan_create_batch(n, dI, dF, dts, None, sp, C.byref(plan)))
     plan_ms = (time.perf_counter() - t0) * 1e3
+    # the batch at the library's default tuning, before autotuning
+    ms_bd = _time_steps(stream, lambda: capi.check(lib.g2g_plan_execute(plan, sp)),
+                        steps, 3)
     tuned = capi.Tuning()
     capi.check(lib.g2g_plan_autotune(plan, sp, 2, C.byref(tuned)))
     capi.check(lib.g2g_plan_capture_graph(plan, sp))
@@ -627,6 +699,11 @@ def run_batched(lib, dev, stream, steps, peak):
     ms_p = _time_steps(stream, plain, max(2, steps // 4), 1)
     ms_m = _time_steps(stream, lambda: capi.check(lib.g2g_plans_execute(n, plans, sp)),
                        steps, 2)
+    # the same tuning policy on both sides: every per-transform plan under the
+    # knobs the autotuner picked for the batch
+    for k in range(n):
+        capi.check(lib.g2g_plan_set_tuning(plans[k], C.byref(tuned)))
+    ms_pt = _time_steps(stream, plain, max(2, steps // 4), 1)
 
     # the reference's calling pattern: one blocking transform call per pair
     # (one-shot API; its plans are cached after the first pass)
@@ -655,15 +732,25 @@ def run_batched(lib, dev, stream, steps, peak):
                                ("tile_bytes", "tile_dim", "ctas_per_sm", "threads", "unroll",
                                 "stages", "ring", "tile_run", "l2_prefetch")},
                     "graph": True},
+        "batched_default_tuning": {"value": round(b / (ms_bd * 1e-3) / 1e9, 2), "unit": UNIT,
+                                   "ms_per_step": round(ms_bd, 4), "launches_per_step": 1,
+                                   "graph": False},
         "plain_launches": {"value": round(b / (ms_p * 1e-3) / 1e9, 2), "unit": UNIT,
                            "ms_per_step": round(ms_p, 4), "launches_per_step": n,
-                           "plan_ms_total": round(plans_ms, 1)},
+                           "plan_ms_total": round(plans_ms, 1),
+                           "tuning": "each plan's default"},
+        "plain_launches_batch_tuning": {"value": round(b / (ms_pt * 1e-3) / 1e9, 2),
+                                        "unit": UNIT, "ms_per_step": round(ms_pt, 4),
+                                        "launches_per_step": n,
+                                        "tuning": "the batch's autotuned knobs"},
         "multi_plan_launch": {"value": round(b / (ms_m * 1e-3) / 1e9, 2), "unit": UNIT,
                               "ms_per_step": round(ms_m, 4), "launches_per_step": 1},
         "plain_calls": {"value": round(b / (ms_c * 1e-3) / 1e9, 2), "unit": UNIT,
                         "ms_per_step": round(ms_c, 4), "launches_per_step": n,
                         "path": "256 blocking g2g_transform calls (plans cached)"},
         "speedup_batched_vs_plain_launches": round(ms_p / ms_b, 3),
+        "speedup_same_tuning": {"default": round(ms_p / ms_bd, 3),
+                                "autotuned": round(ms_pt / ms_b, 3)},
         "speedup_batched_vs_plain_calls": round(ms_c / ms_b, 3),
     }, (w, di, df, dI, dF, dts, keep)
 

@@ -706,7 +706,7 @@ g2g_status plan_on_device(g2g_plan &pl) {
     if (e == cudaSuccess)
         e = cudaMemsetAsync(base + o_counters, 0, 64, ds->plan_stream);
     if (e == cudaSuccess)
-        e = g2g::launch_plan(d, pl.n_pairs, 0, pl.n_cells, ds->plan_stream);
+        e = g2g::launch_plan(d, pl.n_pairs, pl.n_cells, ds->plan_stream);
     long long counters[5] = {0, 0, 0, 0, 0};
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(pinned, base + o_counters, 40, cudaMemcpyDeviceToHost,
@@ -779,6 +779,18 @@ g2g::PlanList single_list(const g2g_plan &pl) {
     l.status = pl.dev.status;
     add_to_list(l, pl);
     return l;
+}
+
+// Launches the gather-scatter over `l`. The TMA-staged kernel is the one that
+// can raise the device status (a bounded wait that expired): its launches
+// clear the status first, so the status always describes the last execution.
+cudaError_t launch_list(const g2g::PlanList &l, const g2g::ScatterConfig &cfg, cudaStream_t s) {
+    if (cfg.stages >= 2 && l.status) {
+        cudaError_t e = cudaMemsetAsync(l.status, 0, sizeof(int), s);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return g2g::launch_scatter(l, cfg, s);
 }
 
 // Configuration that covers every plan of a multi-plan launch: the union of
@@ -986,6 +998,15 @@ g2g_status cached_one_shot(const Sig *key, const std::function<g2g_status(g2g_pl
         if (e != cudaSuccess)
             st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
     }
+    if (st == G2G_SUCCESS && plan->n_tiles > 0 && scatter_config(*plan).stages >= 2) {
+        // the staged kernel records an expired bounded wait in the status
+        int dst = 0;
+        cudaError_t e = cudaMemcpy(&dst, plan->dev.status, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            st = fail(G2G_ERROR_CUDA, "transform status: %s", cudaGetErrorString(e));
+        else if (dst != 0)
+            st = fail(G2G_ERROR_TIMEOUT, "transform: a bounded wait of the staged kernel expired");
+    }
     if (cached) {
         std::lock_guard<std::mutex> lk(g_cache.mu);
         auto it = g_cache.map.find(sig);
@@ -1070,7 +1091,7 @@ g2g_status g2g_plan_execute(g2g_plan *plan, void *stream) {
         if (plan->graph && plan->graph_stream == s) {
             G2G_CUDA(cudaGraphLaunch(plan->graph, s));
         } else {
-            G2G_CUDA(g2g::launch_scatter(single_list(*plan), scatter_config(*plan), s));
+            G2G_CUDA(launch_list(single_list(*plan), scatter_config(*plan), s));
         }
     }
     G2G_CUDA(cudaEventRecord(plan->done, s));
@@ -1108,7 +1129,7 @@ g2g_status g2g_plans_execute(int32_t n_plans, g2g_plan *const *plans, void *stre
                     add_to_list(l, *p);
             }
             if (l.n > 0)
-                G2G_CUDA(g2g::launch_scatter(l, merged_config(grp.data() + base, n), s));
+                G2G_CUDA(launch_list(l, merged_config(grp.data() + base, n), s));
         }
     }
     for (int k = 0; k < n_plans; ++k) {
@@ -1134,7 +1155,7 @@ g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream) {
         return G2G_SUCCESS;
     cudaGraph_t g = nullptr;
     G2G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t le = g2g::launch_scatter(single_list(*plan), scatter_config(*plan), s);
+    cudaError_t le = launch_list(single_list(*plan), scatter_config(*plan), s);
     cudaError_t ee = cudaStreamEndCapture(s, &g);
     G2G_CUDA(le);
     G2G_CUDA(ee);

@@ -28,8 +28,8 @@ struct PlanDevice {
 };
 
 // Runs the device planner (merge, tile counts, scan, emission) on `stream`.
-cudaError_t launch_plan(const PlanDevice &d, int n_pairs, int unused,
-                        long long n_cells, cudaStream_t stream);
+cudaError_t launch_plan(const PlanDevice &d, int n_pairs, long long n_cells,
+                        cudaStream_t stream);
 long long scan_sums_capacity(long long n_cells);
 
 // Grid cover (interval_cover form) of split vector a by b, device arrays.

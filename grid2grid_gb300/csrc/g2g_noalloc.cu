@@ -142,7 +142,7 @@ extern "C" g2g_status g2g_transform_noalloc(const g2g_layout_desc *initial,
                                      cudaMemcpyHostToDevice, s));
     // the previous call's counters are still in the array: clear them
     NOALLOC_CUDA(cudaMemsetAsync(base + o_counters, 0, 64, s));
-    NOALLOC_CUDA(g2g::launch_plan(d, (int)img.pairs.size(), 0, img.n_cells, s));
+    NOALLOC_CUDA(g2g::launch_plan(d, (int)img.pairs.size(), img.n_cells, s));
     long long counters[5] = {0, 0, 0, 0, 0};
     NOALLOC_CUDA(cudaMemcpyAsync(counters, base + o_counters, sizeof(counters),
                                  cudaMemcpyDeviceToHost, s));

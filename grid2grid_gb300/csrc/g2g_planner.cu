@@ -350,9 +350,8 @@ __global__ void cover_kernel(const int32_t *__restrict__ a, int na,
 
 } // namespace
 
-cudaError_t launch_plan(const PlanDevice &d, int n_pairs, int max_nrp_ncp_threads,
-                        long long n_cells, cudaStream_t stream) {
-    (void)max_nrp_ncp_threads;
+cudaError_t launch_plan(const PlanDevice &d, int n_pairs, long long n_cells,
+                        cudaStream_t stream) {
     merge_parts_kernel<<<dim3(n_pairs, 2), 256, 0, stream>>>(d.pairs, d.splits, d.parts);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess)

@@ -22,7 +22,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libg2g_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libg2g_ref.so")
-REF_ROOT = os.environ.get("G2G_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: $G2G_REFERENCE_ROOT, else a sibling of this repository
+REF_ROOT = os.environ.get("G2G_REFERENCE_ROOT",
+                          os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
 
 _port = None
 _ref = None

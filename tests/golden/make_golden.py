@@ -4,7 +4,7 @@ Runs kabicm/grid2grid's own transform (compiled unmodified from its sources
 over the thread-MPI shim, oracle/_ref/libg2g_ref.so) on small seeded cases and
 stores inputs and outputs, so the tests can pin the oracle port and the GPU
 path on machines where the reference is absent. Needs the reference checkout
-(default /root/reference, or $G2G_REFERENCE_ROOT):
+($G2G_REFERENCE_ROOT, else a `reference` folder beside this repository):
 
     python tests/golden/make_golden.py
 

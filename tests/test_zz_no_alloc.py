@@ -3,9 +3,9 @@ device memory (their application owns all of HBM through its own pool, or
 runs under a strict memory quota, or cannot take cudaFree's implicit device
 synchronisation). Its plan metadata lives in a fixed array inside the
 library instead of a per-call allocation. Its results must equal those of
-g2g_transform (bit-exact, the tolerance every parity test here uses) on two
-calls in a row, which also checks that a call does not depend on what the
-previous call left in the shared array.
+g2g_transform and of the oracle port (bit-exact, the tolerance every parity
+test here uses) on two calls in a row, which also checks that a call does not
+depend on what the previous call left in the shared array.
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test; it also passes alone in a fresh process."""
@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import g2g_testlib as T
+import oracle
 from grid2grid_gb300 import capi
 from grid2grid_gb300 import layouts as Ls
 
@@ -28,6 +29,7 @@ def _setup():
     from grid2grid_gb300 import build
     build.build()
     capi.load()
+    oracle.build_port()
 
 
 def _run(entry, Li, Lf, ai, af, op):
@@ -64,6 +66,8 @@ def test_noalloc_matches_transform_on_two_calls_in_a_row():
         want = _run("g2g_transform", Li, Lf, ai, af, op)
         got = _run("g2g_transform_noalloc", Li, Lf, ai, af, op)
         T.assert_arenas_equal(got, want, Lf, what=f"noalloc {op}")
+        port = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+        T.assert_arenas_equal(got, port, Lf, what=f"noalloc vs port {op}")
     # the same transform twice in a row
     Li, Lf, ai, af = first
     want = _run("g2g_transform", Li, Lf, ai, af, ("N", 1.0, 0.0))
@@ -72,10 +76,58 @@ def test_noalloc_matches_transform_on_two_calls_in_a_row():
         T.assert_arenas_equal(got, want, Lf, what="noalloc repeat")
 
 
+def _finite(L, rng):
+    comp = np.float32 if L.dtype in (capi.FLOAT32, capi.COMPLEX64) else np.float64
+    w = np.dtype(comp).itemsize
+    return np.frombuffer(rng.standard_normal(L.arena_bytes // w).astype(comp).tobytes(),
+                         np.uint8).copy()
+
+
+@pytest.mark.parametrize("dt,op", [(capi.FLOAT64, ("T", 1.0, 0.0)),
+                                   (capi.FLOAT32, ("N", 2.0, 0.5)),
+                                   (capi.COMPLEX64, ("C", complex(0.5, -1.0), complex(2.0, 0.25))),
+                                   (capi.COMPLEX128, ("T", -1.5, 0.0))])
+def test_noalloc_scaled_and_transposed_match_port(dt, op):
+    """'T', 'C' and alpha/beta != (1, 0) through the no-allocation call, on
+    finite values: bit-exact against the oracle port and g2g_transform."""
+    rng = np.random.default_rng(90 + dt)
+    Li, Lf, _, _ = _case(30 + dt, dt, op[0], 413, 291)
+    ai, af = _finite(Li, rng), _finite(Lf, rng)
+    port = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+    for _ in range(2):
+        got = _run("g2g_transform_noalloc", Li, Lf, ai, af, op)
+        T.assert_arenas_equal(got, port, Lf, what=f"noalloc vs port dt{dt} {op}")
+    want = _run("g2g_transform", Li, Lf, ai, af, op)
+    T.assert_arenas_equal(got, want, Lf, what=f"noalloc vs transform dt{dt} {op}")
+
+
+def test_noalloc_layouts_in_pinned_host_memory():
+    """Both layouts in pinned host memory: the kernel reads and writes them in
+    place over the host link; the result equals the oracle port's."""
+    import torch
+    lib = capi.load()
+    Li, Lf, ai, af = _case(44, capi.COMPLEX64, "T", 377, 255)
+    op = ("T", 1.0, 0.0)
+    port = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+    hi = torch.from_numpy(ai.copy()).pin_memory()
+    hf = torch.from_numpy(af.copy()).pin_memory()
+    dI, k1 = Li.desc(hi.data_ptr())
+    dF, k2 = Lf.desc(hf.data_ptr())
+    s = torch.cuda.current_stream()
+    for _ in range(2):
+        hf.copy_(torch.from_numpy(af))
+        capi.check(lib.g2g_transform_noalloc(C.byref(dI), C.byref(dF), capi.COMPLEX64,
+                                             C.byref(capi.make_op(*op)),
+                                             C.c_void_p(s.cuda_stream)))
+        T.assert_arenas_equal(hf.numpy(), port, Lf, what="noalloc pinned host")
+
+
 def test_noalloc_rejects_a_plan_larger_than_its_scratch():
-    # a 65536 x 65536 grid of 1 x 1 blocks needs far more metadata than the
-    # fixed array holds; descriptors point at a dummy device buffer and the
-    # call must fail before any device work
+    # a 4096 x 1 grid of 1 x 1 blocks into a 1 x 4096 grid: the cover has
+    # (4096 + 1 + 1) x (1 + 4096 + 1) cells, ~16.8 M, and the planner keeps
+    # two 8-byte counts per cell (~268 MB), far more than the fixed 32 MiB
+    # array holds; descriptors point at a dummy device buffer and the call
+    # must fail before any device work
     import torch
     lib = capi.load()
     buf = torch.zeros(16, dtype=torch.uint8, device="cuda")
