@@ -30,6 +30,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3",
 CU_FLAGS = ARCH + COMMON + ["-Xptxas", "-O3"]
 
 SOURCES = ["g2g_capi.cpp", "g2g_server.cpp", "g2g_scalapack.cpp", "g2g_reorder.cpp",
+           "g2g_exchange.cpp",
            "g2g_planner.cu",
            "g2g_scatter.cu",
            "g2g_scatter_256.cu", "g2g_scatter_512.cu", "g2g_scatter_256e.cu",

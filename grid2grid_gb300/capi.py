@@ -156,6 +156,17 @@ class ScalapackDesc(C.Structure):
     ]
 
 
+class ExchangePiece(C.Structure):
+    _fields_ = [
+        ("row_start", C.c_int32), ("row_end", C.c_int32),
+        ("col_start", C.c_int32), ("col_end", C.c_int32),
+        ("src_rank", C.c_int32), ("dst_rank", C.c_int32),
+        ("offset", C.c_int64),
+    ]
+
+
+EXCHANGE_LOCAL, EXCHANGE_SEND, EXCHANGE_RECV = 0, 1, 2
+
 SIGNATURES = [
     ("g2g_last_error_string", C.c_char_p, []),
     ("g2g_version_string", C.c_char_p, []),
@@ -201,6 +212,19 @@ SIGNATURES = [
       C.POINTER(_VP), C.c_int32, C.c_int32, C.POINTER(ScalapackDesc), _I32P,
       C.POINTER(_VP), C.c_int32, C.c_int32, C.POINTER(ScalapackDesc), _I32P,
       C.c_int, C.POINTER(Op), _VP]),
+    ("g2g_exchange_create", C.c_int,
+     [C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op), C.c_int32,
+      _I32P, C.c_int32, C.POINTER(_VP)]),
+    ("g2g_exchange_get_counts", C.c_int,
+     [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("g2g_exchange_get_rank_counts", C.c_int, [_VP, C.c_int32, C.POINTER(C.c_int64)]),
+    ("g2g_exchange_get_pieces", C.c_int,
+     [_VP, C.c_int32, C.c_int64, C.POINTER(ExchangePiece), C.POINTER(C.c_int64)]),
+    ("g2g_exchange_bind", C.c_int, [_VP, _VP, _VP, _VP]),
+    ("g2g_exchange_pack", C.c_int, [_VP, _VP]),
+    ("g2g_exchange_unpack", C.c_int, [_VP, _VP]),
+    ("g2g_exchange_get_plan_info", C.c_int, [_VP, C.c_int32, C.POINTER(PlanInfo)]),
+    ("g2g_exchange_destroy", C.c_int, [_VP]),
     ("g2g_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(_VP)]),
     ("g2g_server_submit", C.c_int,
      [_VP, C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int, C.POINTER(Op),

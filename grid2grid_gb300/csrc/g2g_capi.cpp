@@ -140,9 +140,14 @@ g2g_status check_splits(const int32_t *s, int n, const char *what, const char *w
 }
 
 // Reads and validates one layout descriptor. `P` is the number of virtual
-// ranks of the transform (the communicator size).
+// ranks of the transform (the communicator size). A partial layout (one
+// shard's part of a layout spread over several processes, or a packed
+// exchange buffer) lists only some blocks: with `held` set, exactly the
+// blocks owned by the ranks r with held[r] != 0; with `absent_ok`, any
+// subset. Blocks not listed take no part in the plan.
 g2g_status load_layout(const g2g_layout_desc *d, const char *which, int P, bool is_final,
-                       int align, HLayout &L) {
+                       int align, HLayout &L, const std::vector<char> *held = nullptr,
+                       bool absent_ok = false) {
     if (!d)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "%s layout descriptor is NULL", which);
     G2G_TRY(check_splits(d->rows_split, d->n_block_rows, "rows", which));
@@ -207,6 +212,11 @@ g2g_status load_layout(const g2g_layout_desc *d, const char *which, int P, bool 
             return fail(G2G_ERROR_INVALID_ARGUMENT,
                         "%s layout: block (%d, %d) is held by rank %d but owned by rank %d",
                         which, bd.row, bd.col, bd.rank, own);
+        if (held && !(*held)[bd.rank])
+            return fail(G2G_ERROR_INVALID_ARGUMENT,
+                        "%s layout: block (%d, %d) of rank %d is listed, but rank %d belongs "
+                        "to another shard",
+                        which, bd.row, bd.col, bd.rank, bd.rank);
         if (is_final && bd.transpose_on_copy)
             return fail(G2G_ERROR_INVALID_ARGUMENT,
                         "final layout: block (%d, %d) is marked transpose_on_copy; a "
@@ -241,9 +251,11 @@ g2g_status load_layout(const g2g_layout_desc *d, const char *which, int P, bool 
         hb.data = (uint64_t)(uintptr_t)bd.data;
         L.blocks[b] = hb;
     }
-    for (size_t k = 0; k < nblk; ++k)
+    for (size_t k = 0; k < nblk && !absent_ok; ++k)
         if (!seen[k]) {
             int i = (int)(k / (size_t)nbc), j = (int)(k % (size_t)nbc);
+            if (held && !(*held)[L.owner(i, j)])
+                continue;
             return fail(G2G_ERROR_INVALID_ARGUMENT,
                         "%s layout: block (%d, %d) owned by rank %d is missing from that "
                         "rank's local blocks",
@@ -284,6 +296,7 @@ struct PairHost {
     bool any_trans = false;
     double alpha[2] = {1, 0}, beta[2] = {0, 0};
     int64_t m = 0, n = 0;
+    int64_t elems = 0; // elements the pair moves: m*n, fewer for a partial plan
 };
 
 g2g_tuning default_tuning() {
@@ -409,7 +422,8 @@ bool cast_supported(int from, int to) {
 }
 
 g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int dtype,
-                      const g2g_op *op, int pair_index, PairHost &p, int src_dtype = -1) {
+                      const g2g_op *op, int pair_index, PairHost &p, int src_dtype = -1,
+                      const g2g::PartialSpec *part = nullptr) {
     (void)pair_index;
     p.dtype = dtype;
     p.esz = dtype_esz(dtype);
@@ -429,8 +443,13 @@ g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int 
     const int P = std::max(1, std::max(di->n_ranks, df->n_ranks));
     // element alignment: that of the real component (float or double)
     auto comp_align = [](int dt) { return (dt == G2G_FLOAT32 || dt == G2G_COMPLEX64) ? 4 : 8; };
-    G2G_TRY(load_layout(di, "initial", P, false, comp_align(p.src_dtype), p.a));
-    G2G_TRY(load_layout(df, "final", P, true, comp_align(dtype), p.b));
+    if (part && ((part->init_held && (int)part->init_held->size() < P) ||
+                 (part->final_held && (int)part->final_held->size() < P)))
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "shard rank sets must cover all %d ranks", P);
+    G2G_TRY(load_layout(di, "initial", P, false, comp_align(p.src_dtype), p.a,
+                        part ? part->init_held : nullptr, part && part->init_absent_ok));
+    G2G_TRY(load_layout(df, "final", P, true, comp_align(dtype), p.b,
+                        part ? part->final_held : nullptr, part && part->final_absent_ok));
     char trans = 'N';
     if (op) {
         trans = (char)std::toupper((unsigned char)op->trans);
@@ -470,6 +489,7 @@ g2g_status build_pair(const g2g_layout_desc *di, const g2g_layout_desc *df, int 
             p.any_trans = true;
     p.m = p.b.rs.back() - p.b.rs.front();
     p.n = p.b.cs.back() - p.b.cs.front();
+    p.elems = (part && part->elems >= 0) ? part->elems : p.m * p.n;
     return G2G_SUCCESS;
 }
 
@@ -553,9 +573,9 @@ void assemble(g2g_plan &pl) {
         pi.alpha[1] = p.alpha[1];
         pi.beta[0] = p.beta[0];
         pi.beta[1] = p.beta[1];
-        const int64_t bytes = p.m * p.n * p.esz;
+        const int64_t bytes = p.elems * p.esz;
         pl.bytes_moved += bytes;
-        pl.bytes_min_traffic += p.cast ? p.m * p.n * (p.src_esz + p.esz)
+        pl.bytes_min_traffic += p.cast ? p.elems * (p.src_esz + p.esz)
                                        : (p.scaled ? 3 : 2) * bytes;
         if (p.any_trans) {
             pl.any_trans = true;
@@ -827,7 +847,8 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
 
 g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layout_desc *finals,
                        const g2g_dtype *dtypes, g2g_dtype single_dtype, const g2g_op *ops,
-                       g2g_plan **out, int src_dtype = -1) {
+                       g2g_plan **out, int src_dtype = -1,
+                       const g2g::PartialSpec *part = nullptr) {
     if (!out)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "plan output pointer is NULL");
     *out = nullptr;
@@ -842,7 +863,7 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
     for (int k = 0; k < n_pairs; ++k) {
         int dt = dtypes ? (int)dtypes[k] : (int)single_dtype;
         g2g_status st = build_pair(&inits[k], &finals[k], dt, ops ? &ops[k] : nullptr, k,
-                                   pl->host[k], src_dtype);
+                                   pl->host[k], src_dtype, part);
         if (st != G2G_SUCCESS) {
             if (n_pairs > 1)
                 t_last_error = "pair " + std::to_string(k) + ": " + t_last_error;
@@ -1428,6 +1449,18 @@ g2g_status build_host_image(const g2g_layout_desc *initial, const g2g_layout_des
     pl.n_tiles = out->tile_capacity; // grid bound only; the launch uses exact counts
     out->cfg = scatter_config(pl);
     return G2G_SUCCESS;
+}
+
+g2g_status create_plan_partial(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                               g2g_dtype dtype, const g2g_op *op, const PartialSpec &part,
+                               g2g_plan **plan) {
+    return create_plan(1, initial, final_, nullptr, dtype, op, plan, -1, &part);
+}
+
+g2g_status validate_partial(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                            g2g_dtype dtype, const g2g_op *op, const PartialSpec &part) {
+    PairHost p;
+    return build_pair(initial, final_, (int)dtype, op, 0, p, -1, &part);
 }
 
 } // namespace g2g

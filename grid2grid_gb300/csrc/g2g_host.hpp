@@ -45,6 +45,27 @@ struct HostPlanImage {
     ScatterConfig cfg;
 };
 
+// A plan over part of a transform: the blocks one shard of a sharded
+// transform holds, or a packed exchange buffer. `init_held` / `final_held`
+// (one entry per virtual rank) name the ranks whose blocks the descriptor
+// lists -- all of them, and no other; `*_absent_ok` lets a descriptor list
+// any subset of blocks. Cells whose source or destination block is not
+// listed take no part. `elems` is the number of elements the plan moves
+// (for its byte counts), -1 for m*n.
+struct PartialSpec {
+    const std::vector<char> *init_held = nullptr;
+    const std::vector<char> *final_held = nullptr;
+    bool init_absent_ok = false;
+    bool final_absent_ok = false;
+    int64_t elems = -1;
+};
+g2g_status create_plan_partial(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                               g2g_dtype dtype, const g2g_op *op, const PartialSpec &part,
+                               g2g_plan **plan);
+// Runs the validation of create_plan_partial without planning.
+g2g_status validate_partial(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                            g2g_dtype dtype, const g2g_op *op, const PartialSpec &part);
+
 // Validates one transform's descriptors exactly as g2g_plan_create does and
 // fills `out`; makes the device holding the blocks current.
 g2g_status build_host_image(const g2g_layout_desc *initial, const g2g_layout_desc *final_,

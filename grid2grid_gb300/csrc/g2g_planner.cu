@@ -135,9 +135,13 @@ __device__ inline bool is_copy_kind(uint32_t kind) {
     return !(kind & (KIND_SCALED | KIND_CAST)) || (kind & KIND_WARP_ELEM);
 }
 
+// A block a partial plan does not hold (one shard's part of a sharded
+// transform, a packed exchange buffer) has a null address in its table; its
+// cells take no part. Every listed block that is not empty has an address.
 __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pairs,
                                   const Part *__restrict__ parts,
                                   const SrcEntry *__restrict__ src_tables,
+                                  const DstEntry *__restrict__ dst_tables,
                                   long long *__restrict__ cell_tiles,
                                   long long *__restrict__ cell_tiles_cta,
                                   unsigned long long *__restrict__ n_pieces) {
@@ -160,7 +164,9 @@ __global__ void cell_tiles_kernel(const PairInfo *__restrict__ pairs, int n_pair
         Part pc = parts[p.col_parts + v];
         long long cnt = 0;
         bool copy = true;
-        if (pr.len > 0 && pc.len > 0) {
+        if (pr.len > 0 && pc.len > 0 &&
+            src_tables[p.src_table + (long long)pr.ia * p.a_nc + pc.ia].data != 0 &&
+            dst_tables[p.dst_table + (long long)pr.ib * p.b_nc + pc.ib].data != 0) {
             const SrcEntry e = src_tables[p.src_table + (long long)pr.ia * p.a_nc + pc.ia];
             uint32_t kind = p.kind | ((e.flags & 1u) ? KIND_TRANS : 0u) |
                             ((e.flags & 2u) ? KIND_CONJ : 0u);
@@ -292,6 +298,8 @@ __global__ void emit_tiles_kernel(const PairInfo *__restrict__ pairs,
             continue;
         const SrcEntry se = src_tables[p.src_table + (long long)pr.ia * p.a_nc + pc.ia];
         const DstEntry de = dst_tables[p.dst_table + (long long)pr.ib * p.b_nc + pc.ib];
+        if (se.data == 0 || de.data == 0) // a block the plan does not hold
+            continue;
         const bool trans = (se.flags & 1u) != 0;
         uint32_t kind = p.kind | (trans ? KIND_TRANS : 0u) | ((se.flags & 2u) ? KIND_CONJ : 0u);
         const int esz = kind_esz(kind), sesz = kind_src_esz(kind);
@@ -363,7 +371,8 @@ cudaError_t launch_plan(const PlanDevice &d, int n_pairs, long long n_cells,
     if (gx < 1)
         gx = 1;
     cell_tiles_kernel<<<dim3(gx, n_pairs), 256, 0, stream>>>(d.pairs, n_pairs, d.parts,
-                                                             d.src_tables, d.cell_tiles,
+                                                             d.src_tables, d.dst_tables,
+                                                             d.cell_tiles,
                                                              d.cell_tiles_cta, d.n_pieces);
     if ((err = cudaGetLastError()) != cudaSuccess)
         return err;

@@ -357,6 +357,89 @@ g2g_status g2g_gemr2d(int32_t m, int32_t n,
                       const g2g_scalapack_desc *desc_b, const int32_t *lld_b,
                       g2g_dtype dtype, const g2g_op *op, void *stream);
 
+/* ---- sharded transform: virtual ranks spread over several GPUs --------- */
+
+/* A transform whose virtual ranks are spread over several GPUs (shards), one
+ * process per GPU, each holding the blocks of its ranks: the reference's
+ * exchange between ranks (exchange_async, transform.cpp:41-124, driven by
+ * communication_data, communication_data.cpp:51-99) with a GPU in place of
+ * an MPI rank. Every shard's process calls these functions with the same
+ * grids, owners, dtype, op and rank-to-shard map, and descriptors that list
+ * exactly the blocks of its own ranks (blocks of other shards' ranks are not
+ * listed). A shard's part is:
+ *   g2g_exchange_pack    local pieces (source and destination rank on this
+ *                        shard) straight into their destination blocks, and
+ *                        pieces bound for other shards, op applied, into the
+ *                        send buffer -- one launch;
+ *   (the caller exchanges the buffers: an all-to-all with the per-shard byte
+ *    counts of g2g_exchange_get_counts, e.g. NCCL);
+ *   g2g_exchange_unpack  received pieces into their destination blocks,
+ *                        alpha/beta applied.
+ * Buffer layout: the section for (or from) shard h starts at the sum of the
+ * byte counts of shards 0..h-1. Inside a section, for each source rank and
+ * then each destination rank (ascending), the pieces between them in the
+ * order of the reference's message sort (column interval, then row
+ * interval; communication_data.cpp:26-30), each packed column-major with its
+ * rows as leading dimension in final orientation: a (source rank,
+ * destination rank) segment holds what the reference's rank sends to the
+ * other in its own buffer. */
+typedef struct g2g_exchange g2g_exchange;
+
+enum { G2G_EXCHANGE_LOCAL = 0, G2G_EXCHANGE_SEND = 1, G2G_EXCHANGE_RECV = 2 };
+
+/* One piece of a shard's part: a cell of the grid cover (both grids' split
+ * points merged), in final coordinates. */
+typedef struct g2g_exchange_piece {
+    int32_t row_start, row_end;  /* [row_start, row_end)                        */
+    int32_t col_start, col_end;  /* [col_start, col_end)                        */
+    int32_t src_rank, dst_rank;  /* owner in the initial (after op) / final grid */
+    int64_t offset;              /* elements from the start of the shard's send
+                                    or receive buffer; -1 for local pieces      */
+} g2g_exchange_piece;
+
+/* Plans shard `shard`'s part of a transform over n_shards shards.
+ * shard_of_rank has one entry per virtual rank (max of both layouts'
+ * n_ranks). Host only: validates the descriptors, computes the grid cover,
+ * the piece lists and counts; no device work. */
+g2g_status g2g_exchange_create(const g2g_layout_desc *initial, const g2g_layout_desc *final_,
+                               g2g_dtype dtype, const g2g_op *op, int32_t n_shards,
+                               const int32_t *shard_of_rank, int32_t shard,
+                               g2g_exchange **ex);
+
+/* Bytes this shard sends to / receives from each shard (n_shards entries
+ * each; the shard's own entries are 0). Either pointer may be NULL. */
+g2g_status g2g_exchange_get_counts(const g2g_exchange *ex, int64_t *send_bytes,
+                                   int64_t *recv_bytes);
+
+/* Elements each virtual rank sends to each other one, over the whole
+ * transform (n_ranks x n_ranks, row-major: counts[s*n_ranks + d]; the
+ * diagonal holds the elements that stay on a rank). Row s, diagonal set to
+ * zero, is the reference's communication_data send counts of rank s
+ * (communication_data.cpp:51-99), column d its receive counts of rank d. */
+g2g_status g2g_exchange_get_rank_counts(const g2g_exchange *ex, int32_t n_ranks,
+                                        int64_t *counts);
+
+/* The local, send or receive pieces (G2G_EXCHANGE_*) of this shard, in
+ * buffer order. pieces may be NULL to ask for the number only. */
+g2g_status g2g_exchange_get_pieces(const g2g_exchange *ex, int32_t which, int64_t capacity,
+                                   g2g_exchange_piece *pieces, int64_t *n_pieces);
+
+/* Binds the device send and receive buffers (at least the sum of the send /
+ * receive byte counts each, element aligned) and plans the local, pack and
+ * unpack gather-scatters on the device. Rebinding replaces the plans. */
+g2g_status g2g_exchange_bind(g2g_exchange *ex, void *send_buffer, void *recv_buffer,
+                             void *stream);
+
+g2g_status g2g_exchange_pack(g2g_exchange *ex, void *stream);
+g2g_status g2g_exchange_unpack(g2g_exchange *ex, void *stream);
+
+/* Plan info of the local, pack (G2G_EXCHANGE_SEND) or unpack
+ * (G2G_EXCHANGE_RECV) gather-scatter; all zero when it has no pieces. */
+g2g_status g2g_exchange_get_plan_info(const g2g_exchange *ex, int32_t which,
+                                      g2g_plan_info *info);
+
+g2g_status g2g_exchange_destroy(g2g_exchange *ex);
+
 /* ---- serving: continuous batching ------------------------------------- */
 
 /* A request loop for transforms of device-resident layouts (no counterpart

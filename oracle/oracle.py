@@ -60,6 +60,11 @@ def port():
             C.c_int, C.POINTER(capi.LayoutDesc), C.POINTER(capi.LayoutDesc),
             C.POINTER(C.c_int), C.POINTER(capi.Op), C.c_int]
         lib.g2g_oracle_last_error.restype = C.c_char_p
+        I64P = C.POINTER(C.c_int64)
+        lib.g2g_oracle_rank_exchange.restype = C.c_int
+        lib.g2g_oracle_rank_exchange.argtypes = [
+            C.POINTER(capi.LayoutDesc), C.POINTER(capi.LayoutDesc), C.c_int,
+            C.POINTER(capi.Op), C.c_int, I64P, I64P, I64P, I64P, C.c_void_p, C.c_int64]
         lib.g2g_oracle_decomp_cover.restype = C.c_int
         lib.g2g_oracle_decomp_cover.argtypes = [
             C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int,
@@ -136,6 +141,34 @@ def port_transform(inits, finals, init_arenas, final_arenas, ops=None, threads=1
     rc = lib.g2g_oracle_transform(len(inits), di, df, dts, opa, int(threads))
     if rc:
         raise RuntimeError("oracle port: " + lib.g2g_oracle_last_error().decode())
+
+
+def port_rank_exchange(Li, Lf, init_arena, final_arena, rank, op=None, pack=True):
+    """The port's communication_data of one rank: send / receive counts and
+    displacements per peer (elements) and its packed send buffer (bytes)."""
+    lib = port()
+    capi = _capi()
+    P = max(1, Li.n_ranks, Lf.n_ranks)
+    di, k1 = _descs([Li], [init_arena])
+    df, k2 = _descs([Lf], [final_arena])
+    arrs = [np.zeros(P, np.int64) for _ in range(4)]
+    I64P = C.POINTER(C.c_int64)
+    o = None if op is None else (op if isinstance(op, capi.Op) else capi.make_op(*op))
+    rc = lib.g2g_oracle_rank_exchange(di, df, Li.dtype, None if o is None else C.byref(o),
+                                      rank, *[a.ctypes.data_as(I64P) for a in arrs], None, 0)
+    if rc:
+        raise RuntimeError("oracle port: " + lib.g2g_oracle_last_error().decode())
+    buf = None
+    if pack:
+        buf = np.zeros(max(1, int(arrs[0].sum())) * Li.esz, np.uint8)
+        rc = lib.g2g_oracle_rank_exchange(di, df, Li.dtype, None if o is None else C.byref(o),
+                                          rank, *[a.ctypes.data_as(I64P) for a in arrs],
+                                          buf.ctypes.data, buf.size)
+        if rc:
+            raise RuntimeError("oracle port: " + lib.g2g_oracle_last_error().decode())
+        buf = buf[: int(arrs[0].sum()) * Li.esz]
+    return {"send_counts": arrs[0], "send_dspls": arrs[1], "recv_counts": arrs[2],
+            "recv_dspls": arrs[3], "send_buffer": buf}
 
 
 # reference call modes (oracle/ref_driver.cpp)

@@ -399,6 +399,55 @@ int transform_pair(const g2g_layout_desc &di, const g2g_layout_desc &df,
     return 0;
 }
 
+// One rank's communication_data (communication_data.cpp:51-99) and packed
+// send buffer (copy_to_buffer, communication_data.cpp:132-142): the piece
+// lists of prepare_to_send / prepare_to_recv (utils.hpp:146-212) sorted by
+// (peer, cols, rows, tag), counts per peer, displacements as exclusive sums.
+template <typename T>
+int rank_exchange(const g2g_layout_desc &di, const g2g_layout_desc &df, const g2g_op *op,
+                  int rank, int64_t *send_counts, int64_t *send_dspls, int64_t *recv_counts,
+                  int64_t *recv_dspls, unsigned char *send_out, int64_t send_capacity) {
+    const int esz = (int)sizeof(T);
+    int P = std::max(1, std::max(di.n_ranks, df.n_ranks));
+    Layout A, B;
+    if (!load_layout(di, P, A) || !load_layout(df, P, B) || rank < 0 || rank >= P) {
+        g_err = "bad layout descriptor or rank";
+        return 1;
+    }
+    char trans = op ? (char)std::toupper((unsigned char)op->trans) : 'N';
+    transpose_layout(A, trans);
+    std::vector<Msg> send, recv;
+    decompose(A.local[rank], A, B, esz, send);
+    decompose(B.local[rank], B, A, esz, recv);
+    std::sort(send.begin(), send.end(), msg_less);
+    std::sort(recv.begin(), recv.end(), msg_less);
+    for (int p = 0; p < P; ++p)
+        send_counts[p] = recv_counts[p] = 0;
+    int64_t total = 0;
+    for (const Msg &m : send)
+        if (m.peer != rank) {
+            if (send_out) {
+                if ((total + m.b.size()) * esz > send_capacity) {
+                    g_err = "send buffer too small";
+                    return 1;
+                }
+                copy_piece<T>(m.b, (T *)(send_out + total * esz), m.b.rows.length(), false,
+                              T{1}, T{0});
+            }
+            total += m.b.size();
+            send_counts[m.peer] += m.b.size();
+        }
+    for (const Msg &m : recv)
+        if (m.peer != rank)
+            recv_counts[m.peer] += m.b.size();
+    send_dspls[0] = recv_dspls[0] = 0;
+    for (int p = 1; p < P; ++p) {
+        send_dspls[p] = send_dspls[p - 1] + send_counts[p - 1];
+        recv_dspls[p] = recv_dspls[p - 1] + recv_counts[p - 1];
+    }
+    return 0;
+}
+
 int transform_dispatch(int dtype, const g2g_layout_desc &di,
                        const g2g_layout_desc &df, const g2g_op *op, int threads) {
     switch (dtype) {
@@ -434,6 +483,35 @@ int g2g_oracle_transform(int n_pairs, const g2g_layout_desc *inits,
             return rc;
     }
     return 0;
+}
+
+// Rank `rank`'s send / receive counts and displacements (P entries each,
+// elements) and, when send_buffer is not NULL, its packed send buffer.
+int g2g_oracle_rank_exchange(const g2g_layout_desc *di, const g2g_layout_desc *df, int dtype,
+                             const g2g_op *op, int rank, int64_t *send_counts,
+                             int64_t *send_dspls, int64_t *recv_counts, int64_t *recv_dspls,
+                             void *send_buffer, int64_t send_capacity_bytes) {
+    g_err.clear();
+    unsigned char *out = (unsigned char *)send_buffer;
+    switch (dtype) {
+    case G2G_FLOAT32:
+        return rank_exchange<float>(*di, *df, op, rank, send_counts, send_dspls, recv_counts,
+                                    recv_dspls, out, send_capacity_bytes);
+    case G2G_FLOAT64:
+        return rank_exchange<double>(*di, *df, op, rank, send_counts, send_dspls, recv_counts,
+                                     recv_dspls, out, send_capacity_bytes);
+    case G2G_COMPLEX64:
+        return rank_exchange<std::complex<float>>(*di, *df, op, rank, send_counts, send_dspls,
+                                                  recv_counts, recv_dspls, out,
+                                                  send_capacity_bytes);
+    case G2G_COMPLEX128:
+        return rank_exchange<std::complex<double>>(*di, *df, op, rank, send_counts, send_dspls,
+                                                   recv_counts, recv_dspls, out,
+                                                   send_capacity_bytes);
+    default:
+        g_err = "bad dtype";
+        return 1;
+    }
 }
 
 // The cover of split vector a by split vector b; returns n_a - 1.
