@@ -406,6 +406,10 @@ def run_ours(args):
                 configs[name] = run_config_leg(lib, name, dev, stream, peak,
                                                max(args.steps, 20))
 
+    sharded = None
+    if args.batch and rank == 0 and w.ops is None and len(w.inits) == 1:
+        sharded = run_sharded_loopback(w, dev, stream, peak, 20)
+
     batched = serving = None
     if args.batch and rank == 0:
         batched, pool = run_batched(lib, dev, stream, 20, peak)
@@ -433,7 +437,8 @@ def run_ours(args):
             "data": "synthetic (seeded random bit patterns, device-resident)",
             "config": _config(w, args), "roofline": roofline, "cpu_baseline": cpu,
             "e2e": e2e, "clocks": clocks, "gpu_launches": args.steps,
-            "configs": configs, "batched_stream": batched, "serving": serving,
+            "configs": configs, "sharded_loopback": sharded,
+            "batched_stream": batched, "serving": serving,
             "scaled": scaled, "cast": cast, "gemr2d": gemr2d,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
@@ -538,6 +543,73 @@ def run_config_leg(lib, name, dev, stream, peak, steps):
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": _profile_traffic("g2g_scatter", name),
                          "algorithmic_bytes_per_launch": info.bytes_min_traffic}}
+
+
+def run_sharded_loopback(w, dev, stream, peak, steps, n_shards=2):
+    """The sharded transform's data path on one GPU: the workload's virtual
+    ranks split into contiguous halves (two shards), each shard's pack
+    (local pieces + send buffer, one launch), the exchange as device-to-device
+    copies of the buffer sections (what an all-to-all between two GPUs would
+    deliver), each shard's unpack. The link between GPUs is not part of it:
+    the time is the HBM work one GPU does for its shard, all shards here."""
+    import torch
+    from grid2grid_gb300 import exchange as X
+    Li, Lf = w.inits[0], w.finals[0]
+    P = max(Li.n_ranks, Lf.n_ranks)
+    smap = X.contiguous_shards(P, n_shards)
+    di, df = _device_arenas(w, dev, 999)
+    shards, keep = [], []
+    for g in range(n_shards):
+        dI, k1 = X.shard_layout(Li, smap, g).desc(di[0].data_ptr())
+        dF, k2 = X.shard_layout(Lf, smap, g).desc(df[0].data_ptr())
+        keep += [k1, k2]
+        shards.append(X.ShardedTransform(dI, dF, Li.dtype, None, smap, g, n_shards, device=dev))
+
+    def exchange():
+        for h, dst in enumerate(shards):
+            pos = 0
+            for g, src in enumerate(shards):
+                n = src.send_bytes[h]
+                if n:
+                    so = sum(src.send_bytes[:h])
+                    dst.recv[pos:pos + n].copy_(src.send[so:so + n])
+                pos += n
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    t = [0.0, 0.0, 0.0]
+    with torch.cuda.stream(stream):
+        for k in range(steps + 3):
+            ev[0].record(stream)
+            for sh in shards:
+                sh.pack(stream)
+            ev[1].record(stream)
+            exchange()
+            ev[2].record(stream)
+            for sh in shards:
+                sh.unpack(stream)
+            ev[3].record(stream)
+            stream.synchronize()
+            if k >= 3:
+                for j in range(3):
+                    t[j] += ev[j].elapsed_time(ev[j + 1]) / steps
+    sent = sum(sum(sh.send_bytes) for sh in shards)
+    ms = sum(t)
+    for sh in shards:
+        sh.close()
+    del di, df
+    torch.cuda.empty_cache()
+    # traffic: every element read and written once (local pieces), or read,
+    # packed, copied, unpacked (remote pieces): 2 bytes per byte moved plus
+    # 4 per byte sent (pack write + copy read/write + unpack read)
+    traffic = 2 * w.bytes_moved + 4 * sent
+    return {"workload": w.name, "shards": n_shards, "rank_to_shard": "contiguous halves",
+            "bytes_moved": w.bytes_moved, "bytes_exchanged": sent,
+            "ms_per_step": round(ms, 4),
+            "ms_pack": round(t[0], 4), "ms_exchange_copies": round(t[1], 4),
+            "ms_unpack": round(t[2], 4),
+            "value": round(w.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
+            "traffic_bytes": traffic,
+            "roofline_frac": round(traffic / (ms * 1e-3) / 1e9 / peak, 4),
+            "note": "one GPU holds every shard; the inter-GPU link is not measured"}
 
 
 def run_scaled(lib, w, dI, dF, dts, stream, peak, steps):

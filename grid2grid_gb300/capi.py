@@ -202,6 +202,9 @@ SIGNATURES = [
      [C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int32, C.POINTER(C.c_int64)]),
     ("g2g_optimal_reordering", C.c_int,
      [C.POINTER(C.c_int64), C.c_int32, _I32P, _I32P]),
+    ("g2g_communication_volume_device", C.c_int,
+     [C.POINTER(LayoutDesc), C.POINTER(LayoutDesc), C.c_int32, _VP, _VP]),
+    ("g2g_optimal_reordering_device", C.c_int, [_VP, C.c_int32, _VP, _VP, _VP]),
     ("g2g_layout_create_scalapack", C.c_int,
      [C.POINTER(ScalapackDesc), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
       C.POINTER(_VP), _I32P, C.c_int, C.POINTER(_VP)]),

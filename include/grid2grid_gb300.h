@@ -311,6 +311,23 @@ g2g_status g2g_communication_volume(const g2g_layout_desc *initial,
 g2g_status g2g_optimal_reordering(const int64_t *volume, int32_t n_ranks,
                                   int32_t *permutation, int32_t *reordered);
 
+/* The two functions above computed on the device, where a sharded
+ * transform keeps its data, to pick the rank-to-GPU map
+ * (transform.cpp:9-39, ranks_reordering.cpp:4-61). `volume` is a DEVICE
+ * array of n_ranks x n_ranks int64 (the layout of g2g_communication_volume),
+ * `permutation` a DEVICE array of n_ranks int32 and `reordered` a DEVICE
+ * int32; both calls are asynchronous on `stream` and give the same results
+ * as the host functions. The matching runs as the locally dominant
+ * matching (every free rank points at its best edge, mutual choices are
+ * matched, repeated), which under the same strict edge order -- weight,
+ * then (r, s) -- is the greedy matching. */
+g2g_status g2g_communication_volume_device(const g2g_layout_desc *initial,
+                                           const g2g_layout_desc *final_, int32_t n_ranks,
+                                           int64_t *volume, void *stream);
+g2g_status g2g_optimal_reordering_device(const int64_t *volume, int32_t n_ranks,
+                                         int32_t *permutation, int32_t *reordered,
+                                         void *stream);
+
 /* ---- ScaLAPACK-descriptor front end ------------------------------------ */
 
 /* A block-cyclic matrix as a ScaLAPACK array descriptor describes it
