@@ -404,7 +404,8 @@ def run_ours(args):
         for name in ("block_cyclic_f64_4096", "transposed_c128_8192"):
             if name != w.name:
                 configs[name] = run_config_leg(lib, name, dev, stream, peak,
-                                               max(args.steps, 20))
+                                               max(args.steps, 20),
+                                               cpu_reps=args.cpu_reps if ws == 1 else 0)
 
     sharded = None
     if args.batch and rank == 0 and w.ops is None and len(w.inits) == 1:
@@ -489,7 +490,7 @@ def _time_steps(stream, fn, steps, warmup):
     return a.elapsed_time(b) / steps
 
 
-def run_config_leg(lib, name, dev, stream, peak, steps):
+def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
     """One single-transform configuration, device-resident, plan cached, one
     launch per step timed with CUDA events on the launching stream. Inputs
     smaller than L2 get it flushed before every step, outside the events (a
@@ -532,9 +533,18 @@ def run_config_leg(lib, name, dev, stream, peak, steps):
     capi.check(lib.g2g_plan_destroy(plan))
     ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
     achieved = info.bytes_min_traffic / (ms * 1e-3) / 1e9
+    cpu = None
+    if cpu_reps > 0:  # the same transform on the host cores, outside the GPU timing
+        threads = _cpu_threads()
+        times, kind, sample = time_cpu_reference(
+            w, cpu_reps, threads, ([t.cpu().numpy() for t in di], [t.cpu().numpy() for t in df]))
+        sec = statistics.median(times)
+        cpu = {"value": round(w.bytes_moved / sec / 1e9, 4), "unit": UNIT, "cores": threads,
+               "kind": kind, "sample": sample}
     del di, df, flush, flush_rd
     torch.cuda.empty_cache()
     return {"workload": name, "config": dict(w.meta), "ms_per_step": round(ms, 5),
+            "cpu_baseline": cpu,
             "value": round(w.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
             "steps": steps, "pieces": info.n_pieces, "tiles": info.n_tiles,
             "l2": "flushed before every step (outside the events)" if small

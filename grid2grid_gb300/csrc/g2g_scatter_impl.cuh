@@ -43,6 +43,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 namespace g2g {
 
 namespace {
@@ -629,6 +631,80 @@ __device__ __forceinline__ void cmul(R a, R b, R c, R d, R &x, R &y) {
         cmul_nan(a, b, c, d, ac, bd, ad, bc, &x, &y);
 }
 
+// Arithmetic with an operand known to be a zero, on the integer pipe. Every
+// result that is not a NaN is the IEEE-754 result bit for bit (signed zeros
+// included); NaN results are NaNs (their payload is left to the
+// implementation, as for the FP pipe's own operations). Selects, no
+// branches: the operands differ from lane to lane.
+template <typename R> struct FBits;
+template <> struct FBits<double> {
+    using U = unsigned long long;
+    static constexpr U SIGN = 0x8000000000000000ull, ABS = 0x7fffffffffffffffull,
+                       INF = 0x7ff0000000000000ull;
+    static __device__ __forceinline__ U get(double v) {
+        return (unsigned long long)__double_as_longlong(v);
+    }
+    static __device__ __forceinline__ double put(U b) { return __longlong_as_double((long long)b); }
+};
+// z * d for a zero z whose sign bit is zs: a NaN when d is infinite or a NaN,
+// else a zero with the sign zs ^ sign(d)
+template <typename R>
+__device__ __forceinline__ R zmul(typename FBits<R>::U zs, R d) {
+    using F = FBits<R>;
+    const typename F::U b = F::get(d);
+    return F::put((b & F::ABS) >= F::INF ? F::ABS /* a quiet NaN */ : ((b & F::SIGN) ^ zs));
+}
+// x + z for z a zero or a NaN: a NaN z gives a NaN, a non-zero x itself, and
+// two zeros -0 only when both are -0 (round to nearest)
+template <typename R> __device__ __forceinline__ R addz(R x, R z) {
+    using F = FBits<R>;
+    const typename F::U bx = F::get(x), bz = F::get(z);
+    const typename F::U r = (bx & F::ABS) != 0 ? bx : (bx & bz & F::SIGN);
+    return F::put((bz & F::ABS) > F::INF ? bz : r);
+}
+template <typename R> __device__ __forceinline__ R subz(R x, R z) {
+    using F = FBits<R>;
+    return addz(x, F::put(F::get(z) ^ F::SIGN));
+}
+
+// (a + b i) * (c + d i) for b a zero (sign bit bs): the two products with b
+// are formed by zmul, the sums with them by addz / subz -- two rounded
+// multiplications instead of four multiplications and two additions, the
+// same result as cmul (the Annex G recovery sees the same values).
+template <typename R>
+__device__ __forceinline__ void cmul_rz(R a, typename FBits<R>::U bs, R c, R d, R &x, R &y) {
+    const R ac = rmul(a, c), ad = rmul(a, d);
+    const R bd = zmul<R>(bs, d), bc = zmul<R>(bs, c);
+    x = subz(ac, bd);
+    y = addz(ad, bc);
+    if (nan_bits(x) && nan_bits(y))
+        cmul_nan(a, FBits<R>::put(bs), c, d, ac, bd, ad, bc, &x, &y);
+}
+// (a + b i) * (c + d i) for a and b both zeros (sign bits as, bs): no
+// rounded operation; the parts are zeros or NaNs (the recovery, reached
+// only for an infinite c or d, multiplies an infinity by a zero)
+template <typename R>
+__device__ __forceinline__ void cmul_zz(typename FBits<R>::U as, typename FBits<R>::U bs, R c,
+                                        R d, R &x, R &y) {
+    const R ac = zmul<R>(as, c), ad = zmul<R>(as, d);
+    const R bd = zmul<R>(bs, d), bc = zmul<R>(bs, c);
+    x = subz(ac, bd);
+    y = addz(ad, bc);
+    if (nan_bits(x) && nan_bits(y))
+        cmul_nan(FBits<R>::put(as), FBits<R>::put(bs), c, d, ac, bd, ad, bc, &x, &y);
+}
+
+// The pair's alpha and beta in the element type, and what is known about
+// them: a real alpha or beta (imaginary part a zero) and a zero beta let
+// complex<double> skip rounded operations whose results are fixed by a zero
+// operand. GB300's FP64 pipe is narrow, and the scaled complex<double> tiles
+// are bound by it.
+enum : uint32_t { COEF_ALPHA_REAL = 1u, COEF_BETA_REAL = 2u, COEF_BETA_ZERO = 4u };
+template <typename T> struct Coef {
+    T alpha, beta;
+    uint32_t zf;
+};
+
 // beta*d + alpha*v, as memory_utils.hpp:36 / :111 / :236 evaluate it.
 __device__ __forceinline__ float axpby(float alpha, float v, float beta, float d) {
     return radd(rmul(beta, d), rmul(alpha, v));
@@ -663,10 +739,94 @@ template <> __device__ __forceinline__ cplxd scalar_from<cplxd>(const double *v)
     return cplxd{v[0], v[1]};
 }
 
+__device__ __forceinline__ bool is_zero_bits(double v) {
+    return (FBits<double>::get(v) & FBits<double>::ABS) == 0;
+}
+template <typename T> __device__ __forceinline__ Coef<T> coef_from(const PairInfo &p) {
+    Coef<T> k;
+    k.alpha = scalar_from<T>(p.alpha);
+    k.beta = scalar_from<T>(p.beta);
+    k.zf = 0;
+    return k;
+}
+template <> __device__ __forceinline__ Coef<cplxd> coef_from<cplxd>(const PairInfo &p) {
+    Coef<cplxd> k;
+    k.alpha = cplxd{p.alpha[0], p.alpha[1]};
+    k.beta = cplxd{p.beta[0], p.beta[1]};
+    k.zf = (is_zero_bits(k.alpha.y) ? COEF_ALPHA_REAL : 0u) |
+           (is_zero_bits(k.beta.y) ? COEF_BETA_REAL : 0u) |
+           (is_zero_bits(k.beta.x) && is_zero_bits(k.beta.y) ? COEF_BETA_ZERO : 0u);
+    return k;
+}
+
+// Which form of beta*d + alpha*v a tile runs (uniform per tile, a template
+// argument of the tile loops so that they stay free of branches): 0 the
+// general one, 1 complex<double> with real alpha and beta, 2 complex<double>
+// with a real alpha and a zero beta. Only complex<double> takes the special
+// forms: the scaled double tiles share their kernel instances with the float
+// ones, whose register allocation an extra form raises (measured: float 'T'
+// with alpha/beta 12 % slower) for a saving of two operations that only
+// pays with a zero beta.
+template <typename T> __device__ __forceinline__ int coef_mode(const Coef<T> &) { return 0; }
+template <> __device__ __forceinline__ int coef_mode<cplxd>(const Coef<cplxd> &k) {
+    const uint32_t real2 = COEF_ALPHA_REAL | COEF_BETA_REAL;
+    if ((k.zf & real2) != real2)
+        return 0;
+    return (k.zf & COEF_BETA_ZERO) ? 2 : 1;
+}
+template <typename T> struct CoefModes { static constexpr bool special = false; };
+template <> struct CoefModes<cplxd> { static constexpr bool special = true; };
+// Calls f(std::integral_constant<int, CM>) with the tile's form.
+template <typename T, typename F>
+__device__ __forceinline__ void coef_dispatch(const Coef<T> &k, F &&f) {
+    if constexpr (CoefModes<T>::special) {
+        const int m = coef_mode<T>(k);
+        if (m == 2) {
+            f(std::integral_constant<int, 2>());
+            return;
+        }
+        if (m == 1) {
+            f(std::integral_constant<int, 1>());
+            return;
+        }
+    }
+    f(std::integral_constant<int, 0>());
+}
+
+template <typename T, int CM> struct AxpbyM {
+    static __device__ __forceinline__ T run(const Coef<T> &k, T v, T d) {
+        return axpby(k.alpha, v, k.beta, d);
+    }
+};
+// complex<double>, real alpha and beta: 6 rounded operations instead of 14
+template <> struct AxpbyM<cplxd, 1> {
+    static __device__ __forceinline__ cplxd run(const Coef<cplxd> &k, cplxd v, cplxd d) {
+        using F = FBits<double>;
+        double bx, by, ax, ay;
+        cmul_rz<double>(k.beta.x, F::get(k.beta.y), d.x, d.y, bx, by);
+        cmul_rz<double>(k.alpha.x, F::get(k.alpha.y), v.x, v.y, ax, ay);
+        return cplxd{radd(bx, ax), radd(by, ay)};
+    }
+};
+// complex<double>, real alpha and zero beta: 2 rounded operations
+template <> struct AxpbyM<cplxd, 2> {
+    static __device__ __forceinline__ cplxd run(const Coef<cplxd> &k, cplxd v, cplxd d) {
+        using F = FBits<double>;
+        double bx, by, ax, ay;
+        cmul_zz<double>(F::get(k.beta.x), F::get(k.beta.y), d.x, d.y, bx, by);
+        cmul_rz<double>(k.alpha.x, F::get(k.alpha.y), v.x, v.y, ax, ay);
+        return cplxd{addz(ax, bx), addz(ay, by)};
+    }
+};
+template <int CM, typename T>
+__device__ __forceinline__ T axpby_m(const Coef<T> &k, T v, T d) {
+    return AxpbyM<T, CM>::run(k, v, d);
+}
+
 // beta*d + alpha*v on the whole elements of a 16-byte chunk.
-template <typename T> __device__ __forceinline__ uint4 axpby_chunk(T alpha, uint4 v, T beta, uint4 d);
-template <>
-__device__ __forceinline__ uint4 axpby_chunk<float>(float alpha, uint4 v, float beta, uint4 d) {
+template <int CM>
+__device__ __forceinline__ uint4 axpby_chunk_t(const Coef<float> &k, uint4 v, uint4 d, float *) {
+    const float alpha = k.alpha, beta = k.beta;
     return make_uint4(
         __float_as_uint(axpby(alpha, __uint_as_float(v.x), beta, __uint_as_float(d.x))),
         __float_as_uint(axpby(alpha, __uint_as_float(v.y), beta, __uint_as_float(d.y))),
@@ -680,15 +840,17 @@ __device__ __forceinline__ void dbl_words(double x, uint32_t &lo, uint32_t &hi) 
     lo = (uint32_t)__double2loint(x);
     hi = (uint32_t)__double2hiint(x);
 }
-template <>
-__device__ __forceinline__ uint4 axpby_chunk<double>(double alpha, uint4 v, double beta, uint4 d) {
+template <int CM>
+__device__ __forceinline__ uint4 axpby_chunk_t(const Coef<double> &k, uint4 v, uint4 d, double *) {
+    const double alpha = k.alpha, beta = k.beta;
     uint4 o;
     dbl_words(axpby(alpha, dbl(v.x, v.y), beta, dbl(d.x, d.y)), o.x, o.y);
     dbl_words(axpby(alpha, dbl(v.z, v.w), beta, dbl(d.z, d.w)), o.z, o.w);
     return o;
 }
-template <>
-__device__ __forceinline__ uint4 axpby_chunk<cplxf>(cplxf alpha, uint4 v, cplxf beta, uint4 d) {
+template <int CM>
+__device__ __forceinline__ uint4 axpby_chunk_t(const Coef<cplxf> &k, uint4 v, uint4 d, cplxf *) {
+    const cplxf alpha = k.alpha, beta = k.beta;
     const cplxf a = axpby(alpha, cplxf{__uint_as_float(v.x), __uint_as_float(v.y)}, beta,
                           cplxf{__uint_as_float(d.x), __uint_as_float(d.y)});
     const cplxf b = axpby(alpha, cplxf{__uint_as_float(v.z), __uint_as_float(v.w)}, beta,
@@ -696,14 +858,18 @@ __device__ __forceinline__ uint4 axpby_chunk<cplxf>(cplxf alpha, uint4 v, cplxf 
     return make_uint4(__float_as_uint(a.x), __float_as_uint(a.y), __float_as_uint(b.x),
                       __float_as_uint(b.y));
 }
-template <>
-__device__ __forceinline__ uint4 axpby_chunk<cplxd>(cplxd alpha, uint4 v, cplxd beta, uint4 d) {
-    const cplxd a = axpby(alpha, cplxd{dbl(v.x, v.y), dbl(v.z, v.w)}, beta,
-                          cplxd{dbl(d.x, d.y), dbl(d.z, d.w)});
+template <int CM>
+__device__ __forceinline__ uint4 axpby_chunk_t(const Coef<cplxd> &k, uint4 v, uint4 d, cplxd *) {
+    const cplxd a = axpby_m<CM>(k, cplxd{dbl(v.x, v.y), dbl(v.z, v.w)},
+                                cplxd{dbl(d.x, d.y), dbl(d.z, d.w)});
     uint4 o;
     dbl_words(a.x, o.x, o.y);
     dbl_words(a.y, o.z, o.w);
     return o;
+}
+template <int CM, typename T>
+__device__ __forceinline__ uint4 axpby_chunk(const Coef<T> &k, uint4 v, uint4 d) {
+    return axpby_chunk_t<CM>(k, v, d, (T *)nullptr);
 }
 
 // A destination read that stays coherent with this kernel's own writes.
@@ -720,9 +886,9 @@ __device__ __forceinline__ uint4 ld_dst_v4(uint64_t addr) {
 // beta*d + alpha*s computed on its elements. Needs every element of the
 // destination to sit inside one 16-byte chunk (its address a multiple of
 // min(sizeof(T), 16)), which scaled_tile checks.
-template <int NWARP, int U, typename T>
-__device__ __forceinline__ void scaled_copy_tile(const Tile &t, const int warp, const T alpha,
-                                                 const T beta) {
+template <int NWARP, int U, typename T, int CM>
+__device__ __forceinline__ void scaled_copy_tile_m(const Tile &t, const int warp,
+                                                   const Coef<T> &cf) {
     const int lane = threadIdx.x & 31;
     const int L = t.rows * (int)sizeof(T);
     if (L <= 0 || t.cols <= 0)
@@ -813,7 +979,7 @@ __device__ __forceinline__ void scaled_copy_tile(const Tile &t, const int warp, 
             }
             const uint32_t m = qm[u] & 15u;
             if (m) {
-                o = axpby_chunk<T>(alpha, o, beta, dd[u]);
+                o = axpby_chunk<CM>(cf, o, dd[u]);
                 if (m == 0xFu) {
                     st_v4(chunk[u], o);
                 } else {
@@ -827,17 +993,24 @@ __device__ __forceinline__ void scaled_copy_tile(const Tile &t, const int warp, 
     }
 }
 
+template <int NWARP, int U, typename T>
+__device__ __forceinline__ void scaled_copy_tile(const Tile &t, const int warp, const Coef<T> &cf) {
+    coef_dispatch(cf, [&](auto cm) {
+        scaled_copy_tile_m<NWARP, U, T, decltype(cm)::value>(t, warp, cf);
+    });
+}
+
 template <int THREADS, typename T>
 __device__ __forceinline__ void scaled_tile(const Tile &t, const PairInfo *pairs,
                                             unsigned char *smem_raw, int td) {
     constexpr int NWARP = THREADS / 32;
     constexpr int E = (int)sizeof(T);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const T alpha = scalar_from<T>(pairs[t.pair].alpha);
-    const T beta = scalar_from<T>(pairs[t.pair].beta);
+    const Coef<T> k = coef_from<T>(pairs[t.pair]);
+    const T alpha = k.alpha, beta = k.beta;
     const int R = t.rows, C = t.cols;
     if ((t.dst & (uint64_t)((E < 16 ? E : 16) - 1)) == 0) { // whole elements per chunk
-        scaled_copy_tile<NWARP, 2, T>(t, warp, alpha, beta);
+        scaled_copy_tile<NWARP, 2, T>(t, warp, k);
         return;
     }
     for (int c = warp; c < C; c += NWARP) {
@@ -1331,10 +1504,10 @@ template <int MODE> __device__ __forceinline__ uint4 ld_dst_elem(uint64_t a) {
 // smem_to_global_m with beta*d + alpha*e on every element, for a tile of
 // 2^rsh rows by 2^csh columns staged [row][column] with a pitch of
 // 2^csh + 1 elements.
-template <int THREADS, int MODE, typename T>
-__device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int rsh, int csh,
-                                                        const unsigned char *smem, T alpha,
-                                                        T beta) {
+template <int THREADS, int MODE, typename T, int CM>
+__device__ __forceinline__ void smem_to_global_scaled_cm(const Tile &t, int rsh, int csh,
+                                                         const unsigned char *smem,
+                                                         const Coef<T> &k) {
     constexpr int ESZ = ModeEsz<MODE>::value;
     static_assert(ESZ == (int)sizeof(T), "element mode matches the element type");
     const int pitch = (1 << csh) + 1;
@@ -1366,11 +1539,19 @@ __device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int rsh, 
                     e.w ^= 0x80000000u;
             }
             const T d = from_words<T>(ld_dst_elem<MODE>(a));
-            st_elem_raw(a, to_words(axpby(alpha, from_words<T>(e), beta, d)), MODE);
+            st_elem_raw(a, to_words(axpby_m<CM>(k, from_words<T>(e), d)), MODE);
         }
         p += cstep * ESZ;
         a += step;
     }
+}
+template <int THREADS, int MODE, typename T>
+__device__ __forceinline__ void smem_to_global_scaled_m(const Tile &t, int rsh, int csh,
+                                                        const unsigned char *smem,
+                                                        const Coef<T> &k) {
+    coef_dispatch(k, [&](auto cm) {
+        smem_to_global_scaled_cm<THREADS, MODE, T, decltype(cm)::value>(t, rsh, csh, smem, k);
+    });
 }
 
 // Stores a scaled transposed (+ conjugated) tile already staged in shared
@@ -1381,28 +1562,22 @@ template <int THREADS, typename T>
 __device__ __forceinline__ void scaled_transpose_store(const Tile &t, const PairInfo *pairs,
                                                        const unsigned char *smem, int td) {
     const int td_shift = td >= 32 ? 5 : 4;
-    const T alpha = scalar_from<T>(pairs[t.pair].alpha);
-    const T beta = scalar_from<T>(pairs[t.pair].beta);
+    const Coef<T> k = coef_from<T>(pairs[t.pair]);
     const int mode = elem_mode(t);
     if constexpr (sizeof(T) == 4) {
-        smem_to_global_scaled_m<THREADS, EM_4, T>(t, td_shift + 1, td_shift + 1, smem, alpha,
-                                                  beta);
+        smem_to_global_scaled_m<THREADS, EM_4, T>(t, td_shift + 1, td_shift + 1, smem, k);
     } else if constexpr (sizeof(T) == 8) {
         if (mode == EM_8)
-            smem_to_global_scaled_m<THREADS, EM_8, T>(t, td_shift + 1, td_shift, smem, alpha,
-                                                      beta);
+            smem_to_global_scaled_m<THREADS, EM_8, T>(t, td_shift + 1, td_shift, smem, k);
         else
-            smem_to_global_scaled_m<THREADS, EM_8_SPLIT, T>(t, td_shift + 1, td_shift, smem,
-                                                            alpha, beta);
+            smem_to_global_scaled_m<THREADS, EM_8_SPLIT, T>(t, td_shift + 1, td_shift, smem, k);
     } else {
         if (mode == EM_16)
-            smem_to_global_scaled_m<THREADS, EM_16, T>(t, td_shift, td_shift, smem, alpha, beta);
+            smem_to_global_scaled_m<THREADS, EM_16, T>(t, td_shift, td_shift, smem, k);
         else if (mode == EM_16_SPLIT8)
-            smem_to_global_scaled_m<THREADS, EM_16_SPLIT8, T>(t, td_shift, td_shift, smem, alpha,
-                                                              beta);
+            smem_to_global_scaled_m<THREADS, EM_16_SPLIT8, T>(t, td_shift, td_shift, smem, k);
         else
-            smem_to_global_scaled_m<THREADS, EM_16_SPLIT4, T>(t, td_shift, td_shift, smem, alpha,
-                                                              beta);
+            smem_to_global_scaled_m<THREADS, EM_16_SPLIT4, T>(t, td_shift, td_shift, smem, k);
     }
 }
 
@@ -1697,23 +1872,19 @@ __device__ __forceinline__ void warp_tile(const Tile &t, int warp, const PairInf
             switch ((t.kind >> KIND_DTYPE_SHIFT) & 3u) {
             case 0:
                 if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
-                    scaled_copy_tile<NWARP, 2, float>(t, warp, scalar_from<float>(pairs[t.pair].alpha),
-                                                      scalar_from<float>(pairs[t.pair].beta));
+                    scaled_copy_tile<NWARP, 2, float>(t, warp, coef_from<float>(pairs[t.pair]));
                 break;
             case 1:
                 if constexpr ((PATHS & PATH_SCALED_REAL) != 0)
-                    scaled_copy_tile<NWARP, 2, double>(t, warp, scalar_from<double>(pairs[t.pair].alpha),
-                                                       scalar_from<double>(pairs[t.pair].beta));
+                    scaled_copy_tile<NWARP, 2, double>(t, warp, coef_from<double>(pairs[t.pair]));
                 break;
             case 2:
                 if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
-                    scaled_copy_tile<NWARP, 2, cplxf>(t, warp, scalar_from<cplxf>(pairs[t.pair].alpha),
-                                                      scalar_from<cplxf>(pairs[t.pair].beta));
+                    scaled_copy_tile<NWARP, 2, cplxf>(t, warp, coef_from<cplxf>(pairs[t.pair]));
                 break;
             default:
                 if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0)
-                    scaled_copy_tile<NWARP, 2, cplxd>(t, warp, scalar_from<cplxd>(pairs[t.pair].alpha),
-                                                      scalar_from<cplxd>(pairs[t.pair].beta));
+                    scaled_copy_tile<NWARP, 2, cplxd>(t, warp, coef_from<cplxd>(pairs[t.pair]));
                 break;
             }
             return;
@@ -2156,12 +2327,10 @@ __device__ __forceinline__ void ring_store(const RingTile &c, RingWalk &w, uint3
 // Stores one landed stage of a scaled tile: each destination chunk becomes
 // beta*d + alpha*s on its whole elements (the pair's alpha and beta, rounded
 // as scaled_copy_tile rounds them), then the chunk walk's word-masked store.
-template <int U, typename T>
-__device__ __forceinline__ void ring_store_scaled(const RingTile &c, RingWalk &w,
-                                                  uint32_t slots, int lane,
-                                                  const PairInfo *pp) {
-    const T alpha = scalar_from<T>(pp->alpha);
-    const T beta = scalar_from<T>(pp->beta);
+template <int U, typename T, int CM>
+__device__ __forceinline__ void ring_store_scaled_m(const RingTile &c, RingWalk &w,
+                                                    uint32_t slots, int lane,
+                                                    const Coef<T> &k) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
         if (w.col < c.cols) {
@@ -2176,7 +2345,7 @@ __device__ __forceinline__ void ring_store_scaled(const RingTile &c, RingWalk &w
                     if (sh)
                         o = funnel_words(o, lds_ring(slot + 16), (uint32_t)(sh >> 2));
                 }
-                o = axpby_chunk<T>(alpha, o, beta, lds_ring(slot + (uint32_t)((U * 32 + 1) * 16)));
+                o = axpby_chunk<CM>(k, o, lds_ring(slot + (uint32_t)((U * 32 + 1) * 16)));
                 const uint64_t chunk = w.d - (uint64_t)d0 + (uint64_t)rel;
                 if (rel >= d0 && rel + 16 <= end) {
                     st_v4(chunk, o);
@@ -2192,6 +2361,15 @@ __device__ __forceinline__ void ring_store_scaled(const RingTile &c, RingWalk &w
         }
         ring_walk_step(w, c);
     }
+}
+template <int U, typename T>
+__device__ __forceinline__ void ring_store_scaled(const RingTile &c, RingWalk &w,
+                                                  uint32_t slots, int lane,
+                                                  const PairInfo *pp) {
+    const Coef<T> k = coef_from<T>(*pp);
+    coef_dispatch(k, [&](auto cm) {
+        ring_store_scaled_m<U, T, decltype(cm)::value>(c, w, slots, lane, k);
+    });
 }
 template <int U, int PATHS>
 __device__ __forceinline__ void ring_store_scaled_dispatch(const RingTile &c, RingWalk &w,

@@ -171,6 +171,52 @@ def test_scaled_tiles_mixed_with_copies_match_port(tuning):
         T.assert_arenas_equal(got[k], want[k], finals[k], what=f"{tuning} case {cases[k]}")
 
 
+def _special_arena(rng, L, dt):
+    """Arena of special operands: signed zeros, infinities, NaNs, subnormals,
+    ones, the largest finite values and normals, each part drawn
+    independently."""
+    comp = np.float32 if dt in (capi.FLOAT32, capi.COMPLEX64) else np.float64
+    fi = np.finfo(comp)
+    pool = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, -np.nan, fi.smallest_subnormal,
+                     -fi.smallest_subnormal, 1.0, -1.0, fi.max, -fi.max, 0.5, -3.25],
+                    dtype=comp)
+    n = L.arena_bytes // np.dtype(comp).itemsize
+    vals = pool[rng.integers(0, len(pool), size=n)]
+    normal = rng.random(n) < 0.3
+    vals[normal] = rng.standard_normal(int(normal.sum())).astype(comp)
+    a = np.zeros(L.arena_bytes, np.uint8)
+    a[:n * np.dtype(comp).itemsize] = np.frombuffer(vals.tobytes(), np.uint8)
+    return a
+
+
+@pytest.mark.parametrize("dt", [capi.FLOAT32, capi.FLOAT64, capi.COMPLEX64, capi.COMPLEX128])
+@pytest.mark.parametrize("t", ["N", "T"])
+def test_real_and_zero_coefficients_on_special_operands(dt, t):
+    """Real alpha / beta (imaginary parts +0 or -0) and zero betas, for which
+    the complex<double> kernels form the products with a zero operand on the
+    integer pipe: signed zeros, infinities, NaNs and subnormals in both
+    operands, bit-exact against the port except NaN payloads."""
+    rng = np.random.default_rng(1200 + 10 * dt + (t == "T"))
+    m, n = 211, 157
+    Li = Ls.random_grid_layout(m if t == "N" else n, n if t == "N" else m, 4, dt, rng,
+                               ext_hi=70)
+    Lf = Ls.random_grid_layout(m, n, 4, dt, rng, ext_hi=70)
+    ai, af = _special_arena(rng, Li, dt), _special_arena(rng, Lf, dt)
+    cplx = dt in (capi.COMPLEX64, capi.COMPLEX128)
+    coefs = [(2.0, 0.5), (-3.0, 0.0), (0.5, -0.0), (1.0, 0.25), (-0.0, 2.0), (0.0, 0.0)]
+    if cplx:
+        coefs += [(complex(2.0, -0.0), complex(0.5, -0.0)),
+                  (complex(-1.5, 0.0), complex(-0.0, -0.0)),
+                  (complex(0.0, -0.0), complex(0.25, 0.0)), (complex(2.0, 1.0), 0.5),
+                  (3.0, complex(0.5, -2.0))]
+    for alpha, beta in coefs:
+        ops = [(t, alpha, beta)]
+        want = T.port_run([Li], [Lf], [ai], [af], ops)[0]
+        got = T.gpu_run([Li], [Lf], [ai], [af], ops)[0]
+        T.assert_arenas_equal(got, want, Lf, nan_equivalent=True,
+                              what=f"dt{dt} {t} alpha={alpha} beta={beta}")
+
+
 def test_scaled_special_values_nan_equivalent():
     """Inf/NaN through alpha/beta (Annex G complex products): equal up to NaN
     payloads, which IEEE leaves to the implementation."""
