@@ -831,10 +831,27 @@ def run_batched(lib, dev, stream, steps, peak):
                         "ms_per_step": round(ms_c, 4), "launches_per_step": n,
                         "path": "256 blocking g2g_transform calls (plans cached)"},
         "speedup_batched_vs_plain_launches": round(ms_p / ms_b, 3),
+        "bound": _batch_bound(w, ms_b, ms_p, peak),
         "speedup_same_tuning": {"default": round(ms_p / ms_bd, 3),
                                 "autotuned": round(ms_pt / ms_b, 3)},
         "speedup_batched_vs_plain_calls": round(ms_c / ms_b, 3),
     }, (w, di, df, dI, dF, dts, keep)
+
+
+def _batch_bound(w, ms_b, ms_p, peak):
+    """What the layout mix allows: the sector-level DRAM traffic floor of the
+    batch (every column's 32-byte sectors once, plus the fills of partial
+    destination sectors next to padding) at the measured copy peak, and the
+    speed-up over the plain launches that a batch at that floor would reach."""
+    from grid2grid_gb300 import workloads as W
+    t = W.sector_traffic(w)
+    floor_ms = t["total"] / (peak * 1e9) * 1e3
+    return {"sector_traffic_bytes": t["total"], "algorithmic_bytes": t["algorithmic"],
+            "traffic_ratio": round(t["total"] / t["algorithmic"], 4),
+            "ms_at_copy_peak": round(floor_ms, 4),
+            "max_speedup_vs_plain_launches": round(ms_p / floor_ms, 3),
+            "copy_peak_fraction_for_3x": round(t["total"] / (ms_p / 3 * 1e-3) / 1e9 / peak, 4),
+            "batched_frac_of_floor": round(floor_ms / ms_b, 4)}
 
 
 def run_serving(lib, pool, rates, duration_s, seed=5):

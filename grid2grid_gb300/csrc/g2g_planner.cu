@@ -113,10 +113,13 @@ __device__ inline void tile_shape(const PairInfo &p, uint32_t kind, int len_r,
         // transposes (plain or scaled) of 4-byte elements take twice the
         // edge, those of 8-byte elements twice the rows: a tile then holds as
         // many bytes as one of 16-byte elements
+        // (4-byte ones are 4 columns short of that: a source line of at
+        // most 2 td - 4 elements at any 4-byte phase lies in the 2 td / 4
+        // aligned 16-byte blocks the line's lanes load, one each)
         const bool shaped = !(kind & KIND_CAST);
         const int esz = kind_esz(kind);
         tr = shaped && esz <= 8 ? 2 * p.tile_dim : p.tile_dim;
-        tc = shaped && esz == 4 ? 2 * p.tile_dim : p.tile_dim;
+        tc = shaped && esz == 4 ? 2 * p.tile_dim - 4 : p.tile_dim;
     } else {
         int esz = kind_esz(kind);
         tr = len_r < p.tile_rows ? len_r : p.tile_rows;

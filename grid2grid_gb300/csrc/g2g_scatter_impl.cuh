@@ -1228,62 +1228,79 @@ __device__ __forceinline__ void smem_to_global(const Tile &t, int td_shift,
 }
 #undef G2G_MODE_DISPATCH
 
-// Plain transposed tiles of 4-byte elements are twice as wide (edge 2 td,
-// shift tsh = td_shift + 1): four elements per 16-byte register slot, so a
-// thread holds 4 NE of them and a CTA keeps as many bytes in flight as with
-// 16-byte elements. Same views as above: loads along source storage
-// columns, stores along destination columns, 4-byte accesses coalesced over
-// the warp.
+// Plain transposed tiles of 4-byte elements are twice as tall and nearly
+// twice as wide (2 td final rows, 2 td - 4 final columns; shift tsh =
+// td_shift + 1 for the 2 td x 2 td shared-memory tile): four elements per
+// 16-byte register slot, so a thread holds 4 NE of them and a CTA keeps as
+// many bytes in flight as with 16-byte elements. A tile line -- one source
+// storage column of up to 2 td - 4 elements -- lies, at any 4-byte phase,
+// in the 2 td / 4 aligned 16-byte blocks starting at its aligned base; the
+// line's 2 td / 4 lanes load one block each, whole, and each block's words
+// go to the elements they hold when the slots are written to shared memory
+// (so the loads stay in flight until then, across the previous tile's
+// stores). The line's bytes are read once, as the sectors that hold them:
+// 4-byte loads at a random phase split every warp request over one more
+// sector than the data holds, and L2 fetched the shared ones twice (reads
+// 1.44x the data on random grids). Stores run along destination columns.
 template <int W> __device__ __forceinline__ void slot_set(uint4 &v, uint32_t x) {
     if (W == 0) v.x = x; else if (W == 1) v.y = x; else if (W == 2) v.z = x; else v.w = x;
 }
 template <int W> __device__ __forceinline__ uint32_t slot_get(const uint4 &v) {
     return W == 0 ? v.x : (W == 1 ? v.y : (W == 2 ? v.z : v.w));
 }
+__device__ __forceinline__ uint32_t slot_word(const uint4 &v, int w) {
+    return w == 0 ? v.x : (w == 1 ? v.y : (w == 2 ? v.z : v.w));
+}
+// Slot i of a thread holds block g of line r0 + i * rstep.
 template <int THREADS, int NE>
 __device__ __forceinline__ void load_slots_w4(const Tile &t, int tsh, uint4 (&v)[NE]) {
-    const int c = threadIdx.x & ((1 << tsh) - 1);
-    const int r0 = threadIdx.x >> tsh;
-    const int rstep = THREADS >> tsh;
-    if (c >= t.cols)
-        return;
-    uint64_t a = t.src + (uint64_t)((long long)r0 * t.src_ld + (long long)c * 4);
-    const uint64_t step = (uint64_t)((long long)rstep * t.src_ld);
+    const int gsh = tsh - 2; // log2 of the lanes per line
+    const int g = threadIdx.x & ((1 << gsh) - 1);
+    const int r0 = threadIdx.x >> gsh;
+    const int rstep = THREADS >> gsh;
+    const int run = t.cols * 4; // bytes of a line
+    const int rel = g << 4;     // this lane's block, from the line's aligned base
 #pragma unroll
     for (int i = 0; i < NE; ++i) {
-#pragma unroll
-        for (int w = 0; w < 4; ++w) {
-            if (r0 + (4 * i + w) * rstep < t.rows) {
-                const uint32_t x = ldg_l1_u32(a);
-                if (w == 0) slot_set<0>(v[i], x);
-                else if (w == 1) slot_set<1>(v[i], x);
-                else if (w == 2) slot_set<2>(v[i], x);
-                else slot_set<3>(v[i], x);
-            }
-            a += step;
-        }
+        const int r = r0 + i * rstep;
+        const uint64_t s = t.src + (uint64_t)((long long)r * t.src_ld);
+        const int ph = (int)(s & 15u);
+        // only blocks holding bytes of the line are read
+        if (r < t.rows && rel < ph + run)
+            v[i] = ldg_v4(s - (uint64_t)ph + (uint64_t)rel);
     }
 }
+// Shared memory [line][element] with a pitch of 2 td + 1 words: word w of
+// block g holds element 4 g + w - q (q the line's phase in words). Lanes
+// g >= 8 write their words in the order 2, 3, 0, 1, so that the lanes of a
+// warp spread over the banks.
 template <int THREADS, int NE>
 __device__ __forceinline__ void slots_to_smem_w4(const Tile &t, int tsh, const uint4 (&v)[NE],
                                                  unsigned char *smem) {
     const int T = 1 << tsh;
-    const int c = threadIdx.x & (T - 1);
-    const int r0 = threadIdx.x >> tsh;
-    const int rstep = THREADS >> tsh;
-    if (c >= t.cols)
-        return;
-    uint32_t *p = reinterpret_cast<uint32_t *>(smem) + r0 * (T + 1) + c;
+    const int gsh = tsh - 2;
+    const int g = threadIdx.x & ((1 << gsh) - 1);
+    const int r0 = threadIdx.x >> gsh;
+    const int rstep = THREADS >> gsh;
+    const bool rot = (g & 8) != 0; // the words in the order 2, 3, 0, 1
+    uint32_t *p = reinterpret_cast<uint32_t *>(smem) + r0 * (T + 1);
     const int step = rstep * (T + 1);
+    uint64_t s = t.src + (uint64_t)((long long)r0 * t.src_ld);
+    const uint64_t sstep = (uint64_t)((long long)rstep * t.src_ld);
 #pragma unroll
     for (int i = 0; i < NE; ++i) {
-#pragma unroll
-        for (int w = 0; w < 4; ++w) {
-            if (r0 + (4 * i + w) * rstep < t.rows)
-                *p = w == 0 ? slot_get<0>(v[i])
-                            : (w == 1 ? slot_get<1>(v[i]) : (w == 2 ? slot_get<2>(v[i]) : slot_get<3>(v[i])));
-            p += step;
+        if (r0 + i * rstep < t.rows) {
+            // element of the first word written, then of the others
+            const int e0 = 4 * g - (int)((s & 15u) >> 2) + (rot ? 2 : 0);
+            const uint4 q = rot ? make_uint4(v[i].z, v[i].w, v[i].x, v[i].y) : v[i];
+            const int e2 = rot ? e0 - 2 : e0 + 2;
+            if (e0 >= 0 && e0 < t.cols) p[e0] = q.x;
+            if (e0 + 1 >= 0 && e0 + 1 < t.cols) p[e0 + 1] = q.y;
+            if (e2 >= 0 && e2 < t.cols) p[e2] = q.z;
+            if (e2 + 1 >= 0 && e2 + 1 < t.cols) p[e2 + 1] = q.w;
         }
+        p += step;
+        s += sstep;
     }
 }
 // Stores of the tall tiles: one warp per destination column, lanes along

@@ -141,6 +141,53 @@ def fill_arenas(w: Workload, seed: int = 7):
     return ia, fa
 
 
+def _column_sectors(L, fills: bool):
+    """32-byte sectors spanned by every stored column of every block of L;
+    with `fills`, also the sectors a column covers only in part where the
+    rest is not the neighbouring column of the same block (padding, another
+    block): writing such a sector makes L2 fetch the rest from DRAM."""
+    esz = L.esz
+    spanned = partial = 0
+    rs, cs = L.rows_split, L.cols_split
+    for b in range(L.n_blocks):
+        i, j = int(L.blocks["row"][b]), int(L.blocks["col"][b])
+        h, w = int(rs[i + 1] - rs[i]), int(cs[j + 1] - cs[j])
+        if L.blocks["trans"][b]:
+            h, w = w, h
+        if h == 0 or w == 0:
+            continue
+        st = int(L.blocks["stride"][b])
+        starts = int(L.offsets[b]) + np.arange(w, dtype=np.int64) * st * esz
+        ends = starts + h * esz
+        first, last = starts // 32, (ends - 1) // 32
+        spanned += int((last - first + 1).sum())
+        if fills:
+            ps, pe = starts % 32 != 0, ends % 32 != 0
+            if st == h:  # columns back to back: inner boundaries meet
+                ps[1:] = False
+                pe[:-1] = False
+            n = ps.astype(np.int64) + pe.astype(np.int64) - ((first == last) & ps & pe)
+            partial += int(n.sum())
+    return spanned * 32, partial * 32
+
+
+def sector_traffic(w: Workload) -> dict:
+    """DRAM bytes any gather-scatter of the workload moves at least: the
+    sectors of every source column read once, of every destination column
+    written once, and one sector read per partial destination sector whose
+    other bytes are not written by the transform (padding, a neighbouring
+    block); with the algorithmic 2 x bytes moved for comparison. Offsets
+    are arena offsets from 256-byte aligned arena bases."""
+    rd = wr = fill = 0
+    for Li, Lf in zip(w.inits, w.finals):
+        rd += _column_sectors(Li, False)[0]
+        a, f = _column_sectors(Lf, True)
+        wr += a
+        fill += f
+    return {"read": rd, "write": wr, "fill": fill, "total": rd + wr + fill,
+            "algorithmic": 2 * w.bytes_moved}
+
+
 BY_NAME = {
     "block_cyclic_f64_4096": block_cyclic_f64_4096,
     "random_grid_f32_16384": random_grid_f32_16384,
