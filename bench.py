@@ -530,8 +530,33 @@ def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
             capi.check(lib.g2g_plan_execute(plan, sp))
             ev[k][1].record(stream)
     stream.synchronize()
-    capi.check(lib.g2g_plan_destroy(plan))
     ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    # plans that qualify also run as 2-D TMA boxes through tensor maps
+    # (cp.async.bulk.tensor loads and stores), timed the same way
+    boxes = None
+    if info.tensor_boxes_ok:
+        t = capi.Tuning()
+        t.tensor_boxes = 1
+        capi.check(lib.g2g_plan_set_tuning(plan, C.byref(t)))
+        with torch.cuda.stream(stream):
+            for _ in range(5):
+                capi.check(lib.g2g_plan_execute(plan, sp))
+            for k in range(steps):
+                if small:
+                    flush.zero_()
+                    flush_rd.sum()
+                ev[k][0].record(stream)
+                capi.check(lib.g2g_plan_execute(plan, sp))
+                ev[k][1].record(stream)
+        stream.synchronize()
+        bms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+        bach = info.bytes_min_traffic / (bms * 1e-3) / 1e9
+        boxes = {"kernel": "tma_box_kernel (cp.async.bulk.tensor 2-D loads and stores)",
+                 "ms_per_step": round(bms, 5),
+                 "value": round(w.bytes_moved / (bms * 1e-3) / 1e9, 2), "unit": UNIT,
+                 "roofline_frac": round(bach / peak, 4),
+                 "traffic": _profile_traffic("tma_box", name)}
+    capi.check(lib.g2g_plan_destroy(plan))
     achieved = info.bytes_min_traffic / (ms * 1e-3) / 1e9
     cpu = None
     if cpu_reps > 0:  # the same transform on the host cores, outside the GPU timing
@@ -544,7 +569,7 @@ def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
     del di, df, flush, flush_rd
     torch.cuda.empty_cache()
     return {"workload": name, "config": dict(w.meta), "ms_per_step": round(ms, 5),
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "tensor_boxes": boxes,
             "value": round(w.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
             "steps": steps, "pieces": info.n_pieces, "tiles": info.n_tiles,
             "l2": "flushed before every step (outside the events)" if small

@@ -34,7 +34,8 @@ SOURCES = ["g2g_capi.cpp", "g2g_server.cpp", "g2g_scalapack.cpp", "g2g_reorder.c
            "g2g_planner.cu",
            "g2g_scatter.cu",
            "g2g_scatter_256.cu", "g2g_scatter_512.cu", "g2g_scatter_256e.cu",
-           "g2g_scatter_512e.cu", "g2g_noalloc.cu", "g2g_volume.cu"]
+           "g2g_scatter_512e.cu", "g2g_noalloc.cu", "g2g_volume.cu",
+           "g2g_tma.cu"]
 HEADERS = ["g2g_internal.hpp", "g2g_launch.hpp", "g2g_host.hpp", "g2g_scatter_impl.cuh"]
 
 

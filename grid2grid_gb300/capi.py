@@ -81,6 +81,7 @@ class Tuning(C.Structure):
         ("ring", C.c_int32),
         ("tile_run", C.c_int32),
         ("l2_prefetch", C.c_int32),
+        ("tensor_boxes", C.c_int32),
     ]
 
 
@@ -128,6 +129,8 @@ class PlanInfo(C.Structure):
         ("metadata_bytes", C.c_int64),
         ("graph_captured", C.c_int32),
         ("device_status", C.c_int32),
+        ("tensor_boxes_ok", C.c_int32),
+        ("reserved_info", C.c_int32),
         ("tuning", Tuning),
     ]
 

@@ -311,6 +311,7 @@ g2g_tuning default_tuning() {
     t.ring = 1;
     t.tile_run = 1;
     t.l2_prefetch = -1;
+    t.tensor_boxes = -1;
     return t;
 }
 
@@ -327,6 +328,7 @@ g2g_tuning merge_tuning(const g2g_tuning &base, const g2g_tuning *over) {
     if (over->ring) t.ring = over->ring;
     if (over->tile_run) t.tile_run = over->tile_run;
     if (over->l2_prefetch) t.l2_prefetch = over->l2_prefetch;
+    if (over->tensor_boxes) t.tensor_boxes = over->tensor_boxes;
     return t;
 }
 
@@ -348,6 +350,8 @@ g2g_status check_tuning(const g2g_tuning &t) {
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tile_run must be a power of two in [1, 64]");
     if (t.l2_prefetch != -1 && t.l2_prefetch != 1)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: l2_prefetch must be -1 or 1");
+    if (t.tensor_boxes != -1 && t.tensor_boxes != 1)
+        return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: tensor_boxes must be -1 or 1");
     if (t.ctas_per_sm < 1 || t.ctas_per_sm > 32)
         return fail(G2G_ERROR_INVALID_ARGUMENT, "tuning: ctas_per_sm outside [1, 32]");
     return G2G_SUCCESS;
@@ -387,6 +391,11 @@ struct g2g_plan {
     cudaEvent_t done = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaStream_t graph_stream = nullptr;
+    // plain copies as tensor-map boxes (built when the tuning first asks)
+    bool tma_ok = false;
+    int tma_esz = 0, tma_box_rows = 0, tma_box_cols = 0;
+    void *tma_mem = nullptr;
+    g2g::TmaPlan tma;
 };
 
 namespace g2g {
@@ -845,6 +854,217 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
     return c;
 }
 
+long long gcd_ll(long long a, long long b) {
+    while (b) {
+        const long long t = a % b;
+        a = b;
+        b = t;
+    }
+    return a < 0 ? -a : a;
+}
+
+// Whether the plan's pieces can move as 2-D tensor-map boxes, and the box:
+// plain copies (no op arithmetic, no transposes, no casts) of one element
+// size between device blocks at 16-byte aligned addresses with strides that
+// are multiples of 16 bytes, every split point of both grids (from the
+// first) a multiple of the box's rows and columns, so that every piece and
+// its offsets in both blocks are whole boxes. A box is 2-16 KB.
+void tma_eligibility(g2g_plan &pl) {
+    pl.tma_ok = false;
+    if (pl.host_memory || pl.n_pairs < 1)
+        return;
+    int esz = 0;
+    long long gr = 0, gc = 0;
+    for (const PairHost &p : pl.host) {
+        if (p.scaled || p.cast || p.any_trans)
+            return;
+        if (esz && p.esz != esz)
+            return;
+        esz = p.esz;
+        for (const HLayout *L : {&p.a, &p.b}) {
+            for (int32_t x : L->rs)
+                gr = gcd_ll(gr, x - L->rs.front());
+            for (int32_t x : L->cs)
+                gc = gcd_ll(gc, x - L->cs.front());
+            for (const HBlock &b : L->blocks)
+                if ((b.data & 15u) != 0 || ((uint64_t)b.stride * (uint64_t)esz) % 16u != 0)
+                    return;
+        }
+    }
+    if (gr <= 0 || gc <= 0)
+        return;
+    // rows: the largest divisor of gr whose bytes are a multiple of 16, at
+    // most 256 map words; columns: the largest divisor of gc up to 256 that
+    // keeps the box within 16 KB
+    const int words_per_elem = esz <= 4 ? 1 : esz / 8;
+    int br = 0;
+    for (long long d = std::min<long long>(gr, 256 / words_per_elem); d >= 1; --d)
+        if (gr % d == 0 && (d * esz) % 16 == 0 && d * esz <= 1024) {
+            br = (int)d;
+            break;
+        }
+    if (!br)
+        return;
+    int bc = 0;
+    for (long long d = std::min<long long>(gc, 256); d >= 1; --d)
+        if (gc % d == 0 && (long long)br * d * esz <= 16384) {
+            bc = (int)d;
+            break;
+        }
+    if (!bc || (long long)br * bc * esz < 2048)
+        return;
+    pl.tma_ok = true;
+    pl.tma_esz = esz;
+    pl.tma_box_rows = br;
+    pl.tma_box_cols = bc;
+}
+
+// The merged partition of two split vectors: (start, length, interval of a,
+// interval of b) of every non-empty part.
+struct HPart {
+    int32_t start, len, ia, ib;
+};
+std::vector<HPart> merge_parts(const std::vector<int32_t> &a, const std::vector<int32_t> &b) {
+    std::vector<HPart> out;
+    size_t i = 0, j = 0;
+    int32_t pos = a.front();
+    while (i + 1 < a.size() && j + 1 < b.size()) {
+        const int32_t end = std::min(a[i + 1], b[j + 1]);
+        if (end > pos)
+            out.push_back({pos, end - pos, (int32_t)i, (int32_t)j});
+        pos = std::max(pos, end);
+        if (a[i + 1] <= pos)
+            ++i;
+        if (j + 1 < b.size() && b[j + 1] <= pos)
+            ++j;
+    }
+    return out;
+}
+
+// Builds the tensor maps and the box list, and uploads them. Blocks of one
+// rank with one stride whose origins lie in the columns of a common array
+// (a ScaLAPACK local array: origin = row offset + column offset x stride)
+// share one map over that array, addressed by the block's row and column
+// offsets in it, so that a launch touches a few descriptors; any other
+// block gets a map of its own.
+g2g_status build_tma(g2g_plan &pl) {
+    if (pl.tma_mem)
+        return G2G_SUCCESS;
+    const int esz = pl.tma_esz, br = pl.tma_box_rows, bc = pl.tma_box_cols;
+    const int word = esz == 4 ? 4 : 8, wpe = esz / word;
+    std::vector<unsigned char> maps;
+    std::vector<g2g::TmaBox> boxes;
+    struct Origin {
+        int32_t map = -1;
+        int64_t x = 0, y = 0; // element row and column of the block in its map
+    };
+    for (const PairHost &p : pl.host) {
+        std::vector<Origin> aorg((size_t)p.a.nbr() * p.a.nbc()),
+            borg((size_t)p.b.nbr() * p.b.nbc());
+        for (int side = 0; side < 2; ++side) {
+            const HLayout &L = side ? p.b : p.a;
+            std::vector<Origin> &org = side ? borg : aorg;
+            // groups of blocks by (rank, stride): the lowest origin is the base
+            std::map<std::pair<int, int64_t>, std::vector<const HBlock *>> groups;
+            for (const HBlock &b : L.blocks) {
+                if (L.rs[b.row + 1] > L.rs[b.row] && L.cs[b.col + 1] > L.cs[b.col])
+                    groups[{b.rank, b.stride}].push_back(&b);
+            }
+            for (auto &g : groups) {
+                const int64_t ld = g.first.second, ldb = ld * esz;
+                uint64_t base = UINT64_MAX;
+                for (const HBlock *b : g.second)
+                    base = std::min<uint64_t>(base, b->data);
+                int64_t max_col = 0;
+                std::vector<const HBlock *> own;
+                std::vector<std::pair<const HBlock *, Origin>> shared;
+                for (const HBlock *b : g.second) {
+                    const uint64_t off = b->data - base;
+                    const int64_t rows = L.rs[b->row + 1] - L.rs[b->row];
+                    const int64_t cols = L.cs[b->col + 1] - L.cs[b->col];
+                    Origin o;
+                    o.y = (int64_t)(off / (uint64_t)ldb);
+                    o.x = (int64_t)((off % (uint64_t)ldb) / (uint64_t)esz);
+                    // (coordinates are 32-bit: far-apart blocks get maps of their own)
+                    if (off % (uint64_t)esz != 0 || o.x + rows > ld ||
+                        o.y + cols > (int64_t)INT32_MAX || (o.x + rows) * wpe > (int64_t)INT32_MAX) {
+                        own.push_back(b);
+                        continue;
+                    }
+                    max_col = std::max(max_col, o.y + cols);
+                    shared.push_back({b, o});
+                }
+                if (!shared.empty()) {
+                    const int32_t idx = (int32_t)(maps.size() / 128);
+                    maps.resize(maps.size() + 128);
+                    cudaError_t e = g2g::encode_box_map(
+                        maps.data() + (size_t)idx * 128, (const void *)(uintptr_t)base, word,
+                        (uint64_t)(ld * wpe), (uint64_t)max_col, (uint64_t)ldb,
+                        (uint32_t)(br * wpe), (uint32_t)bc);
+                    if (e != cudaSuccess)
+                        return fail(G2G_ERROR_CUDA, "tensor map of a local array: %s",
+                                    cudaGetErrorString(e));
+                    for (auto &so : shared) {
+                        so.second.map = idx;
+                        org[(size_t)so.first->row * L.nbc() + so.first->col] = so.second;
+                    }
+                }
+                for (const HBlock *b : own) {
+                    const int64_t rows = L.rs[b->row + 1] - L.rs[b->row];
+                    const int64_t cols = L.cs[b->col + 1] - L.cs[b->col];
+                    const int32_t idx = (int32_t)(maps.size() / 128);
+                    maps.resize(maps.size() + 128);
+                    cudaError_t e = g2g::encode_box_map(
+                        maps.data() + (size_t)idx * 128, (const void *)(uintptr_t)b->data, word,
+                        (uint64_t)(rows * wpe), (uint64_t)cols, (uint64_t)ldb,
+                        (uint32_t)(br * wpe), (uint32_t)bc);
+                    if (e != cudaSuccess)
+                        return fail(G2G_ERROR_CUDA, "tensor map of a block: %s",
+                                    cudaGetErrorString(e));
+                    Origin o;
+                    o.map = idx;
+                    org[(size_t)b->row * L.nbc() + b->col] = o;
+                }
+            }
+        }
+        const std::vector<HPart> rp = merge_parts(p.a.rs, p.b.rs);
+        const std::vector<HPart> cp = merge_parts(p.a.cs, p.b.cs);
+        for (const HPart &c : cp)
+            for (const HPart &r : rp) {
+                const Origin &so = aorg[(size_t)r.ia * p.a.nbc() + c.ia];
+                const Origin &dn = borg[(size_t)r.ib * p.b.nbc() + c.ib];
+                if (so.map < 0 || dn.map < 0)
+                    continue;
+                const int64_t sr = so.x + r.start - p.a.rs[r.ia], sc = so.y + c.start - p.a.cs[c.ia];
+                const int64_t dr = dn.x + r.start - p.b.rs[r.ib], dc = dn.y + c.start - p.b.cs[c.ib];
+                for (int32_t j = 0; j < c.len; j += bc)
+                    for (int32_t i = 0; i < r.len; i += br)
+                        boxes.push_back({so.map, dn.map, (int32_t)((sr + i) * wpe),
+                                         (int32_t)(sc + j), (int32_t)((dr + i) * wpe),
+                                         (int32_t)(dc + j)});
+            }
+    }
+    const size_t maps_bytes = (maps.size() + 255) / 256 * 256;
+    const size_t total = maps_bytes + boxes.size() * sizeof(g2g::TmaBox);
+    G2G_CUDA(cudaMalloc(&pl.tma_mem, std::max<size_t>(total, 256)));
+    cudaError_t e = cudaMemcpy(pl.tma_mem, maps.data(), maps.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !boxes.empty())
+        e = cudaMemcpy((char *)pl.tma_mem + maps_bytes, boxes.data(),
+                       boxes.size() * sizeof(g2g::TmaBox), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(pl.tma_mem);
+        pl.tma_mem = nullptr;
+        G2G_CUDA(e);
+    }
+    pl.tma.maps = (const unsigned char *)pl.tma_mem;
+    pl.tma.boxes = (const g2g::TmaBox *)((char *)pl.tma_mem + maps_bytes);
+    pl.tma.n_boxes = (long long)boxes.size();
+    pl.tma.box_bytes = br * bc * esz;
+    return G2G_SUCCESS;
+}
+
+bool use_tma(const g2g_plan &pl) { return pl.tma_ok && pl.tuning.tensor_boxes == 1; }
+
 g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layout_desc *finals,
                        const g2g_dtype *dtypes, g2g_dtype single_dtype, const g2g_op *ops,
                        g2g_plan **out, int src_dtype = -1,
@@ -894,6 +1114,7 @@ g2g_status create_plan(int n_pairs, const g2g_layout_desc *inits, const g2g_layo
         pl->tuning.threads = cta_tiles ? 256 : 512;
         pl->tuning.ctas_per_sm = cta_tiles ? 3 : 2;
     }
+    tma_eligibility(*pl);
     G2G_CUDA(cudaEventCreateWithFlags(&pl->done, cudaEventDisableTiming));
 
     *out = pl;
@@ -1019,8 +1240,10 @@ g2g_status cached_one_shot(const Sig *key, const std::function<g2g_status(g2g_pl
         if (e != cudaSuccess)
             st = fail(G2G_ERROR_CUDA, "transform failed: %s", cudaGetErrorString(e));
     }
-    if (st == G2G_SUCCESS && plan->n_tiles > 0 && scatter_config(*plan).stages >= 2) {
-        // the staged kernel records an expired bounded wait in the status
+    if (st == G2G_SUCCESS && plan->n_tiles > 0 &&
+        (scatter_config(*plan).stages >= 2 || use_tma(*plan))) {
+        // the staged and tensor-box kernels record an expired bounded wait
+        // in the status
         int dst = 0;
         cudaError_t e = cudaMemcpy(&dst, plan->dev.status, sizeof(int), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess)
@@ -1111,6 +1334,10 @@ g2g_status g2g_plan_execute(g2g_plan *plan, void *stream) {
     if (plan->n_tiles > 0) {
         if (plan->graph && plan->graph_stream == s) {
             G2G_CUDA(cudaGraphLaunch(plan->graph, s));
+        } else if (use_tma(*plan)) {
+            G2G_TRY(build_tma(*plan));
+            G2G_CUDA(cudaMemsetAsync(plan->dev.status, 0, sizeof(int), s));
+            G2G_CUDA(g2g::launch_tma_boxes(plan->tma, plan->sm_count, plan->dev.status, s));
         } else {
             G2G_CUDA(launch_list(single_list(*plan), scatter_config(*plan), s));
         }
@@ -1175,8 +1402,17 @@ g2g_status g2g_plan_capture_graph(g2g_plan *plan, void *stream) {
     if (plan->n_tiles == 0)
         return G2G_SUCCESS;
     cudaGraph_t g = nullptr;
+    if (use_tma(*plan))
+        G2G_TRY(build_tma(*plan)); // uploads happen before the capture
     G2G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    cudaError_t le = launch_list(single_list(*plan), scatter_config(*plan), s);
+    cudaError_t le = cudaSuccess;
+    if (use_tma(*plan)) {
+        le = cudaMemsetAsync(plan->dev.status, 0, sizeof(int), s);
+        if (le == cudaSuccess)
+            le = g2g::launch_tma_boxes(plan->tma, plan->sm_count, plan->dev.status, s);
+    } else {
+        le = launch_list(single_list(*plan), scatter_config(*plan), s);
+    }
     cudaError_t ee = cudaStreamEndCapture(s, &g);
     G2G_CUDA(le);
     G2G_CUDA(ee);
@@ -1258,9 +1494,15 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
                                         t.ring = rg;
                                         t.tile_run = run;
                                         t.l2_prefetch = pf;
+                                        t.tensor_boxes = -1;
                                         cands.push_back(t);
                                     }
         }
+    if (plan->tma_ok) { // the tensor-box kernel takes none of the other knobs
+        g2g_tuning t = start;
+        t.tensor_boxes = 1;
+        cands.push_back(t);
+    }
     cudaEvent_t e0, e1;
     G2G_CUDA(cudaEventCreate(&e0));
     G2G_CUDA(cudaEventCreate(&e1));
@@ -1305,6 +1547,7 @@ g2g_status g2g_plan_get_info(const g2g_plan *plan, g2g_plan_info *info) {
     info->bytes_min_traffic = plan->bytes_min_traffic;
     info->metadata_bytes = (int64_t)plan->dmem_bytes;
     info->graph_captured = plan->graph ? 1 : 0;
+    info->tensor_boxes_ok = plan->tma_ok ? 1 : 0;
     info->tuning = plan->tuning;
     if (plan->dev.status) {
         G2G_CUDA(cudaSetDevice(plan->device));
@@ -1335,6 +1578,12 @@ g2g_status g2g_plan_destroy(g2g_plan *plan) {
             if (e != cudaSuccess)
                 st = fail(G2G_ERROR_CUDA, "cudaFreeAsync failed: %s", cudaGetErrorString(e));
         }
+    }
+    if (plan->tma_mem) {
+        cudaSetDevice(plan->device);
+        if (plan->done)
+            cudaEventSynchronize(plan->done);
+        cudaFree(plan->tma_mem);
     }
     if (plan->done)
         cudaEventDestroy(plan->done);

@@ -110,6 +110,29 @@ size_t transpose_smem_bytes(int tile_dim, int esz);
 cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,
                            cudaStream_t stream);
 
+// Plain copies as 2-D tensor-map boxes (g2g_tma.cu). One box moves a
+// box_rows x box_cols sub-block from the source block's tensor map at
+// (sx, sy) to the destination block's at (dx, dy); coordinates are in map
+// words (4 or 8 bytes) along the rows and in columns.
+struct TmaBox {
+    int32_t src_map, dst_map; // indices into the plan's tensor maps (128 B each)
+    int32_t sx, sy, dx, dy;
+};
+struct TmaPlan {
+    const unsigned char *maps = nullptr; // device, 128-byte tensor maps
+    const TmaBox *boxes = nullptr;       // device work list
+    long long n_boxes = 0;
+    int box_bytes = 0;
+};
+// Encodes a 2-D tensor map over a column-major block: rows_words words of
+// word_bytes (4 or 8) per column, `cols` columns ld_bytes apart, boxes of
+// box_rows_words x box_cols. Host only (driver entry point).
+cudaError_t encode_box_map(void *map, const void *base, int word_bytes, uint64_t rows_words,
+                           uint64_t cols, uint64_t ld_bytes, uint32_t box_rows_words,
+                           uint32_t box_cols);
+size_t tma_smem_bytes(int box_bytes);
+cudaError_t launch_tma_boxes(const TmaPlan &p, int sm_count, int *status, cudaStream_t s);
+
 // Prepares every kernel instance a plan or a merged launch can select on the
 // current device (dry runs of launch_scatter), so that no later launch pays
 // for loading its module lazily.

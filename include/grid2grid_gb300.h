@@ -142,6 +142,13 @@ typedef struct g2g_tuning {
     int32_t l2_prefetch;      /* ring: 1 = a warp entering a tile asks L2 for
                                  the tile's source columns in bulk, -1 = no
                                  (0 = default: no)                          */
+    int32_t tensor_boxes;     /* plain copies of a plan whose blocks are
+                                 16-byte aligned with 16-byte multiple strides
+                                 and whose pieces are whole boxes of one shape
+                                 (e.g. block-cyclic to block-cyclic): 1 = move
+                                 them as 2-D TMA boxes through tensor maps,
+                                 -1 = no (0 = default: no); ignored when the
+                                 plan does not qualify                      */
 } g2g_tuning;
 
 typedef struct g2g_plan_info {
@@ -156,6 +163,8 @@ typedef struct g2g_plan_info {
     int32_t device_status;    /* 0, or the error a kernel of the plan raised
                                  (1 = a bounded wait expired); reading it
                                  synchronises with the plan's last execution */
+    int32_t tensor_boxes_ok;  /* 1 if the plan qualifies for tensor_boxes    */
+    int32_t reserved_info;
     g2g_tuning tuning;        /* knobs in effect                             */
 } g2g_plan_info;
 
