@@ -413,7 +413,8 @@ def run_ours(args):
 
     batched = serving = None
     if args.batch and rank == 0:
-        batched, pool = run_batched(lib, dev, stream, 20, peak)
+        batched, pool = run_batched(lib, dev, stream, 20, peak,
+                                    cpu_reps=args.cpu_reps if ws == 1 else 0)
         if args.serving:
             serving = run_serving(lib, pool, [1000, 5000, 20000], 1.0)
         del pool
@@ -759,7 +760,7 @@ def run_cast_only(args):
     return 0
 
 
-def run_batched(lib, dev, stream, steps, peak):
+def run_batched(lib, dev, stream, steps, peak, cpu_reps=0):
     """uneven_batch_256: 256 redistributions of uneven shapes and dtypes.
     batched = one plan over all pairs (the vector transform), autotuned and
     replayed as a captured CUDA graph: ONE launch per step.
@@ -828,6 +829,14 @@ def run_batched(lib, dev, stream, steps, peak):
         capi.check(lib.g2g_plan_destroy(plans[k]))
     capi.check(lib.g2g_plan_destroy(plan))
     b = w.bytes_moved
+    # the same 256 transforms on the host cores (one pass after a warm-up)
+    cpu = None
+    if cpu_reps > 0:
+        threads = _cpu_threads()
+        times, kind, sample = time_cpu_reference(
+            w, 1, threads, ([t.cpu().numpy() for t in di], [t.cpu().numpy() for t in df]))
+        cpu = {"value": round(b / statistics.median(times) / 1e9, 4), "unit": UNIT,
+               "cores": threads, "kind": kind, "sample": sample}
     return {
         "workload": w.name, "bytes_per_step": b, "pieces": info.n_pieces,
         "tiles": info.n_tiles,
@@ -860,6 +869,7 @@ def run_batched(lib, dev, stream, steps, peak):
         "speedup_same_tuning": {"default": round(ms_p / ms_bd, 3),
                                 "autotuned": round(ms_pt / ms_b, 3)},
         "speedup_batched_vs_plain_calls": round(ms_c / ms_b, 3),
+        "cpu_baseline": cpu,
     }, (w, di, df, dI, dF, dts, keep)
 
 
