@@ -315,12 +315,16 @@ def run_ours(args):
             setattr(t, k.strip(), int(v))
         capi.check(lib.g2g_plan_set_tuning(plan, C.byref(t)))
     tuned = None
-    if args.autotune:
+    default_ms = None
+    if args.autotune and not args.tuning:
+        # the library's autotuner picks the knobs of the cached plan before the
+        # timed region (the default tuning's time is reported beside)
+        default_ms = _plan_kernel_ms(plan, sp, stream, 10, w.bytes_moved < 512 * 2**20, dev)
         t = capi.Tuning()
         capi.check(lib.g2g_plan_autotune(plan, sp, 3, C.byref(t)))
         tuned = {k: getattr(t, k) for k in ("tile_bytes", "tile_dim", "ctas_per_sm",
                                             "threads", "unroll", "stages", "ring",
-                                            "tile_run", "l2_prefetch")}
+                                            "tile_run", "l2_prefetch", "tensor_boxes")}
     info = capi.PlanInfo()
     capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
     # warm-up
@@ -444,15 +448,39 @@ def run_ours(args):
             "scaled": scaled, "cast": cast, "gemr2d": gemr2d,
             "plan": {"pieces": info.n_pieces, "tiles": info.n_tiles,
                      "create_ms": round(plan_ms, 3), "autotuned": tuned,
+                     "default_tuning_kernel_ms": default_ms,
                      "tuning": {k: getattr(info.tuning, k) for k in
                                 ("tile_bytes", "tile_dim", "ctas_per_sm", "threads",
-                                 "unroll", "stages", "ring", "tile_run", "l2_prefetch")}},
+                                 "unroll", "stages", "ring", "tile_run", "l2_prefetch",
+                                 "tensor_boxes")}},
         }
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def _plan_kernel_ms(plan, sp, stream, steps, flush_l2, dev):
+    """Mean CUDA-event time of one execution of `plan` (L2 flushed before
+    each when the working set fits in it)."""
+    import torch
+    from grid2grid_gb300 import capi
+    lib = capi.load()
+    flush = torch.empty(512 * 2**20, dtype=torch.uint8, device=dev) if flush_l2 else None
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            capi.check(lib.g2g_plan_execute(plan, sp))
+        for a, b in ev:
+            if flush is not None:
+                flush.zero_()
+            a.record(stream)
+            capi.check(lib.g2g_plan_execute(plan, sp))
+            b.record(stream)
+    stream.synchronize()
+    return round(statistics.mean(a.elapsed_time(b) for a, b in ev), 5)
 
 
 def _device_arenas(w, dev, seed):
@@ -1111,7 +1139,9 @@ def main(argv=None):
     ap.add_argument("--workload", default="random_grid_f32_16384")
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-reps", type=int, default=2)
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="time the main plan at the library's default tuning instead of "
+                         "the knobs its autotuner picks")
     ap.add_argument("--tuning", default="", metavar="K=V,...",
                     help="g2g_tuning fields for the main plan (e.g. stages=3 for the "
                          "TMA-staged kernel)")
