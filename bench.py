@@ -722,9 +722,13 @@ def run_cast(lib, dev, stream, peak, steps, m=16384):
         capi.check(lib.g2g_plan_create_cast(di, dts, df, dtd, None, sp, C.byref(plan)))
         info = capi.PlanInfo()
         capi.check(lib.g2g_plan_get_info(plan, C.byref(info)))
+        ms_default = _time_steps(stream, lambda: capi.check(lib.g2g_plan_execute(plan, sp)),
+                                 steps, 3)
+        t = capi.Tuning()  # the plan's knobs picked by the autotuner, as for the main plan
+        capi.check(lib.g2g_plan_autotune(plan, sp, 2, C.byref(t)))
         ms = _time_steps(stream, lambda: capi.check(lib.g2g_plan_execute(plan, sp)), steps, 3)
         capi.check(lib.g2g_plan_destroy(plan))
-        out[name] = {"ms_per_step": round(ms, 4),
+        out[name] = {"ms_per_step": round(ms, 4), "ms_default_tuning": round(ms_default, 4),
                      "value": round(info.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
                      "traffic_bytes": info.bytes_min_traffic,
                      "roofline_frac": round(info.bytes_min_traffic / (ms * 1e-3) / 1e9 / peak, 4)}
