@@ -316,7 +316,9 @@ def run_ours(args):
         capi.check(lib.g2g_plan_set_tuning(plan, C.byref(t)))
     tuned = None
     default_ms = None
-    if args.autotune and not args.tuning:
+    # the autotuner times repeated executions back to back, so for a working
+    # set that fits in L2 it would rank L2 hits: those plans keep the default
+    if args.autotune and not args.tuning and w.bytes_moved >= 512 * 2**20:
         # the library's autotuner picks the knobs of the cached plan before the
         # timed region (the default tuning's time is reported beside)
         default_ms = _plan_kernel_ms(plan, sp, stream, 10, w.bytes_moved < 512 * 2**20, dev)
