@@ -47,7 +47,7 @@ cudaError_t kernel_occupancy(const void *fn, int threads, size_t smem, int *occ)
 size_t transpose_smem_bytes(int tile_dim, int esz) {
     // room for the plain transposed tiles of 4-byte elements (twice the
     // edge) and of 8-byte ones (twice the rows) too
-    const size_t wide = (size_t)(2 * tile_dim) * (size_t)(2 * tile_dim + 1) * 4u;
+    const size_t wide = ((size_t)(2 * tile_dim) * (size_t)(2 * tile_dim + 1) + 4u) * 4u;
     const size_t tall = (size_t)(2 * tile_dim) * (size_t)(tile_dim + 1) * 8u;
     const size_t own = (size_t)tile_dim * (size_t)(tile_dim + 1) * (size_t)esz;
     const size_t m = wide > tall ? wide : tall;

@@ -1270,10 +1270,16 @@ __device__ __forceinline__ void load_slots_w4(const Tile &t, int tsh, uint4 (&v)
             v[i] = ldg_v4(s - (uint64_t)ph + (uint64_t)rel);
     }
 }
-// Shared memory [line][element] with a pitch of 2 td + 1 words: word w of
-// block g holds element 4 g + w - q (q the line's phase in words). Lanes
-// g >= 8 write their words in the order 2, 3, 0, 1, so that the lanes of a
-// warp spread over the banks.
+// Shared memory [line][element] with a pitch of 2 td + 1 words, after a
+// guard of 4 words: word w of block g holds element 4 g + w - q (q the
+// line's phase in words). Lanes g >= 8 write their words in the order
+// 2, 3, 0, 1, so that the lanes of a warp spread over the banks. Every word
+// of every slot is written, unchecked: elements -3..-1 of a line fall on
+// words 2 td - 2 .. 2 td of the line before (or the guard), elements from
+// t.cols up on words of the line past its last element, and lines past
+// t.rows inside the tile; a line holds at most 2 td - 4 elements, so none of
+// those words is read back (slots not loaded hold unspecified words).
+constexpr int kW4Guard = 4; // words ahead of line 0
 template <int THREADS, int NE>
 __device__ __forceinline__ void slots_to_smem_w4(const Tile &t, int tsh, const uint4 (&v)[NE],
                                                  unsigned char *smem) {
@@ -1283,22 +1289,23 @@ __device__ __forceinline__ void slots_to_smem_w4(const Tile &t, int tsh, const u
     const int r0 = threadIdx.x >> gsh;
     const int rstep = THREADS >> gsh;
     const bool rot = (g & 8) != 0; // the words in the order 2, 3, 0, 1
-    uint32_t *p = reinterpret_cast<uint32_t *>(smem) + r0 * (T + 1);
+    uint32_t *p = reinterpret_cast<uint32_t *>(smem) + kW4Guard + r0 * (T + 1) + 4 * g +
+                  (rot ? 2 : 0);
     const int step = rstep * (T + 1);
     uint64_t s = t.src + (uint64_t)((long long)r0 * t.src_ld);
     const uint64_t sstep = (uint64_t)((long long)rstep * t.src_ld);
 #pragma unroll
     for (int i = 0; i < NE; ++i) {
-        if (r0 + i * rstep < t.rows) {
-            // element of the first word written, then of the others
-            const int e0 = 4 * g - (int)((s & 15u) >> 2) + (rot ? 2 : 0);
-            const uint4 q = rot ? make_uint4(v[i].z, v[i].w, v[i].x, v[i].y) : v[i];
-            const int e2 = rot ? e0 - 2 : e0 + 2;
-            if (e0 >= 0 && e0 < t.cols) p[e0] = q.x;
-            if (e0 + 1 >= 0 && e0 + 1 < t.cols) p[e0 + 1] = q.y;
-            if (e2 >= 0 && e2 < t.cols) p[e2] = q.z;
-            if (e2 + 1 >= 0 && e2 + 1 < t.cols) p[e2 + 1] = q.w;
-        }
+        if (r0 + i * rstep >= T) // lines past the tile's 2 td (td = 16)
+            break;
+        // first word written, then the others
+        uint32_t *w = p - (int)((s & 15u) >> 2);
+        const uint4 q = rot ? make_uint4(v[i].z, v[i].w, v[i].x, v[i].y) : v[i];
+        uint32_t *w2 = rot ? w - 2 : w + 2;
+        w[0] = q.x;
+        w[1] = q.y;
+        w2[0] = q.z;
+        w2[1] = q.w;
         p += step;
         s += sstep;
     }
@@ -1340,7 +1347,7 @@ __device__ __forceinline__ void smem_to_global_w4(const Tile &t, int tsh,
     const int cstep = THREADS >> tsh;
     if (r >= t.rows)
         return;
-    const uint32_t *p = reinterpret_cast<const uint32_t *>(smem) + r * (T + 1) + c0;
+    const uint32_t *p = reinterpret_cast<const uint32_t *>(smem) + kW4Guard + r * (T + 1) + c0;
     uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 4);
     const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
 #pragma unroll
@@ -1535,7 +1542,9 @@ __device__ __forceinline__ void smem_to_global_scaled_cm(const Tile &t, int rsh,
     if (r >= t.rows)
         return;
     const bool conj = (t.kind & KIND_CONJ) != 0;
-    const unsigned char *p = smem + (size_t)(r * pitch + c0) * ESZ;
+    // (4-byte tiles come in the wide layout, after its guard words)
+    const unsigned char *p =
+        smem + (ESZ == 4 ? kW4Guard * 4 : 0) + (size_t)(r * pitch + c0) * ESZ;
     uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ESZ);
     const uint64_t step = (uint64_t)((long long)cstep * t.dst_ld);
     // the destination elements are pulled into L1 together (prefetches hold
@@ -1783,8 +1792,11 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
 // CTA-level tiles (transposed, and scaled or cast ones that are not
 // warp-level) of a launch, static striding, with the next plain transposed
 // tile's loads issued before the current tile is stored.
-template <int THREADS, int PATHS>
-__device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
+// The tile edge is a template argument (TDS = log2 td): every lane mapping,
+// pitch and loop bound of the tile helpers is then a constant.
+template <int THREADS, int PATHS, int TDS>
+__device__ __forceinline__ void cta_phase_t(const PlanList &list, unsigned char *smem) {
+    constexpr int td = 1 << TDS;
     constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
     // Kernels with scaled or cast tiles move plain transposed tiles one at a
     // time: the next tile's loads held across their element code would cost
@@ -1792,7 +1804,7 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
     constexpr bool PIPE = (PATHS & PATH_TRANSPOSE) && !(PATHS & (PATH_SCALED | PATH_CAST));
     // kernels with element arithmetic take every plain transposed shape
     constexpr bool NARROW = (PATHS & (PATH_NARROW_TRANSPOSE | PATH_SCALED | PATH_CAST)) != 0;
-    const int td_shift = td >= 32 ? 5 : 4;
+    constexpr int td_shift = TDS;
     const long long n = list.total_cta;
     const long long G = gridDim.x;
     uint4 v[NE];
@@ -1849,6 +1861,14 @@ __device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *s
         }
         ti = next;
     }
+}
+
+template <int THREADS, int PATHS>
+__device__ __forceinline__ void cta_phase(const PlanList &list, unsigned char *smem, int td) {
+    if (td >= 32)
+        cta_phase_t<THREADS, PATHS, 5>(list, smem);
+    else
+        cta_phase_t<THREADS, PATHS, 4>(list, smem);
 }
 
 // A non-transposed cast tile from source type S on the register path.
