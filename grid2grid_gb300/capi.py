@@ -130,7 +130,7 @@ class PlanInfo(C.Structure):
         ("graph_captured", C.c_int32),
         ("device_status", C.c_int32),
         ("tensor_boxes_ok", C.c_int32),
-        ("reserved_info", C.c_int32),
+        ("tile_paths", C.c_int32),
         ("tuning", Tuning),
     ]
 

@@ -54,6 +54,10 @@ size_t transpose_smem_bytes(int tile_dim, int esz) {
     return own > m ? own : m;
 }
 
+size_t staged_transpose_w4_smem_bytes(int tile_dim) {
+    return w4_staged_smem_bytes(tile_dim);
+}
+
 int stage_bytes_for(int tile_bytes) {
     const long long b = (long long)tile_bytes * 9 / 8 + 512;
     return (int)((b + 127) / 128 * 128);
@@ -109,6 +113,7 @@ cudaError_t preload_scatter_kernels() {
     const int path_sets[] = {PATH_COPY, PATH_TRANSPOSE, PATH_COPY | PATH_TRANSPOSE,
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
                              PATH_COPY | PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
+                             PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W4_STAGED,
                              PATH_COPY | PATH_SCALED_REAL, PATH_COPY | PATH_SCALED_COMPLEX,
                              PATH_COPY | PATH_CAST};
     for (int threads : {256, 512})
@@ -124,6 +129,8 @@ cudaError_t preload_scatter_kernels() {
                     c.paths = paths;
                     c.tile_dim = 32;
                     c.trans_bytes = c.smem_bytes = transpose_smem_bytes(32, 16);
+                    if (paths & PATH_W4_STAGED)
+                        c.smem_bytes = w4_staged_smem_bytes(32);
                     c.ring = mode == 1;
                     c.stages = mode >= 2 ? mode : 0;
                     c.stage_bytes = stage_bytes_for(16 * 1024);

@@ -59,8 +59,10 @@ enum : int {
     PATH_SCALED_COMPLEX = 8, // scaled complex tiles (more registers)
     PATH_SCALED = PATH_SCALED_REAL | PATH_SCALED_COMPLEX,
     PATH_CAST = 16,          // tiles converting the element type
-    PATH_NARROW_TRANSPOSE = 32 // plain transposed tiles of 4- or 8-byte elements
-                               // (the wide and tall tile shapes)
+    PATH_NARROW_TRANSPOSE = 32, // plain transposed tiles of 4- or 8-byte elements
+                                // (the wide and tall tile shapes)
+    PATH_W4_STAGED = 64 // every CTA-level tile a plain transpose of 4-byte
+                        // elements, staged raw through a cp.async ring
 };
 
 // ---------------------------------------------------------------- memory ops
@@ -72,6 +74,16 @@ __device__ __forceinline__ uint4 ldg_v4(uint64_t addr) {
     return v;
 }
 
+__device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gaddr)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 __device__ __forceinline__ void st_v4(uint64_t addr, uint4 v) {
     asm volatile("st.global.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(addr), "r"(v.x), "r"(v.y),
                  "r"(v.z), "r"(v.w)
@@ -1789,6 +1801,108 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
                                       : MinBlocks<U, THREADS>::value;
 };
 
+// Plain transposed tiles of 4-byte elements when they are the launch's only
+// CTA-level tiles (PATH_W4_STAGED): the tile's source lines are copied raw
+// into a ring of kW4Stages shared-memory stages with cp.async (the line's
+// 2 td / 4 aligned 16-byte blocks, one per lane, as the register path loads
+// them), so that a CTA keeps the next kW4Stages - 1 tiles in flight while it
+// stores the current one, without holding them in registers; the stores
+// read each element at its line's phase. A stage is 2 td lines of 2 td + 4
+// words (16-byte aligned lines; a line's elements sit at words q .. q +
+// cols - 1, q its phase in words, and cols <= 2 td - 4).
+constexpr int kW4Stages = 3;
+template <int T> struct W4Stage {
+    static constexpr int pitch = T + 4; // words per line
+    static constexpr int bytes = T * pitch * 4;
+};
+__host__ __device__ constexpr size_t w4_staged_smem_bytes(int td) {
+    return (size_t)kW4Stages * (size_t)(2 * td) * (size_t)(2 * td + 4) * 4u;
+}
+// Issues the copies of tile t's source lines into the stage at shared
+// address st (one 16-byte block per lane and pass; blocks past the line's
+// last element and lines past t.rows are not copied).
+template <int THREADS, int T>
+__device__ __forceinline__ void w4_issue(const Tile &t, uint32_t st) {
+    constexpr int G = T / 4;                          // lanes (blocks) per line
+    constexpr int RSTEP = THREADS / G;                // lines per pass
+    constexpr int NP = (T + RSTEP - 1) / RSTEP;       // passes
+    constexpr int P = W4Stage<T>::pitch;
+    const int g = threadIdx.x % G;
+    const int r0 = threadIdx.x / G;
+    const int run = t.cols * 4;
+    const int rel = g * 16;
+    uint64_t s = t.src + (uint64_t)((long long)r0 * t.src_ld);
+    const uint64_t sstep = (uint64_t)((long long)RSTEP * t.src_ld);
+    uint32_t d = st + (uint32_t)((r0 * P + 4 * g) * 4);
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const int ph = (int)(s & 15u);
+        if (r0 + i * RSTEP < t.rows && rel < ph + run)
+            cp_async16(d, s - (uint64_t)ph + (uint64_t)rel);
+        s += sstep;
+        d += (uint32_t)(RSTEP * P * 4);
+    }
+}
+// Stores tile t from its stage: a thread per final row (source line) r,
+// columns c0, c0 + CSTEP, ...; element c of line r is word q_r + c.
+template <int THREADS, int T>
+__device__ __forceinline__ void w4_store(const Tile &t, const uint32_t *st) {
+    constexpr int CSTEP = THREADS / T;
+    constexpr int NC = (T - 4 + CSTEP - 1) / CSTEP;
+    constexpr int P = W4Stage<T>::pitch;
+    const int r = threadIdx.x % T;
+    const int c0 = threadIdx.x / T;
+    if (r >= t.rows)
+        return;
+    const uint64_t s = t.src + (uint64_t)((long long)r * t.src_ld);
+    const uint32_t *p = st + r * P + (int)((s & 15u) >> 2) + c0;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 4);
+    const uint64_t step = (uint64_t)((long long)CSTEP * t.dst_ld);
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        if (c0 + i * CSTEP < t.cols)
+            st_u32(a, p[i * CSTEP]);
+        a += step;
+    }
+}
+// The CTA's tiles ti = blockIdx.x + k G in order: tile k sits in stage
+// k % S; at step k the CTA waits for its own copies of tile k, meets at a
+// barrier (tile k's lines are then visible to all its threads, and every
+// thread has stored tile k - 1), refills stage (k - 1) % S with tile
+// k + S - 1 and stores tile k. Every step commits one copy group (empty
+// when no tile is left), so the wait always counts S - 2 younger groups.
+template <int THREADS, int TDS>
+__device__ __forceinline__ void cta_phase_w4(const PlanList &list, unsigned char *smem) {
+    constexpr int T = 2 << TDS; // 2 td lines per tile
+    constexpr int S = kW4Stages;
+    constexpr int SB = W4Stage<T>::bytes;
+    const long long n = list.total_cta;
+    const long long G = gridDim.x;
+    const uint32_t base = smem_addr(smem);
+    const PairInfo *unused;
+#pragma unroll
+    for (int k = 0; k < S - 1; ++k) {
+        const long long ti = (long long)blockIdx.x + (long long)k * G;
+        if (ti < n)
+            w4_issue<THREADS, T>(*locate_cta(list, ti, unused), base + (uint32_t)(k * SB));
+        cp_async_commit();
+    }
+    int st = 0;
+    for (long long ti = blockIdx.x; ti < n; ti += G) {
+        cp_async_wait<S - 2>();
+        __syncthreads();
+        const long long nx = ti + (long long)(S - 1) * G;
+        const int sn = st == 0 ? S - 1 : st - 1;
+        if (nx < n)
+            w4_issue<THREADS, T>(*locate_cta(list, nx, unused), base + (uint32_t)(sn * SB));
+        cp_async_commit();
+        w4_store<THREADS, T>(*locate_cta(list, ti, unused),
+                             reinterpret_cast<const uint32_t *>(smem + st * SB));
+        st = st + 1 == S ? 0 : st + 1;
+    }
+    cp_async_wait<0>();
+}
+
 // CTA-level tiles (transposed, and scaled or cast ones that are not
 // warp-level) of a launch, static striding, with the next plain transposed
 // tile's loads issued before the current tile is stored.
@@ -1796,6 +1910,10 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
 // pitch and loop bound of the tile helpers is then a constant.
 template <int THREADS, int PATHS, int TDS>
 __device__ __forceinline__ void cta_phase_t(const PlanList &list, unsigned char *smem) {
+    if constexpr ((PATHS & PATH_W4_STAGED) != 0) {
+        cta_phase_w4<THREADS, TDS>(list, smem);
+        return;
+    }
     constexpr int td = 1 << TDS;
     constexpr int NE = 1024 / THREADS; // slots for a 32 x 32 tile
     // Kernels with scaled or cast tiles move plain transposed tiles one at a
@@ -2007,16 +2125,6 @@ __host__ __device__ constexpr int ring_extra_rows(int paths) {
     return (paths & PATH_SCALED) ? 1 : ((paths & PATH_CAST) ? 2 : 0);
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t saddr, uint64_t gaddr) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(gaddr)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-    asm volatile("cp.async.commit_group;" ::: "memory");
-}
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 // ring reads, ordered after the wait and warp barrier that make them valid
 __device__ __forceinline__ uint32_t lds_ring_u32(uint32_t a) {
     uint32_t v;
@@ -2773,6 +2881,12 @@ template <int THREADS>
 cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
     if (cfg.paths == PATH_COPY)
         return launch_u<THREADS, PATH_COPY>(l, cfg, s);
+    // transposes of 4-byte elements only: the staged ring (no copy tiles, so
+    // the unroll knob has nothing to act on)
+    if ((cfg.paths & PATH_W4_STAGED) &&
+        (cfg.paths & ~(PATH_W4_STAGED | PATH_NARROW_TRANSPOSE)) == PATH_TRANSPOSE)
+        return launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W4_STAGED>(
+            l, cfg, s);
     const bool narrow = (cfg.paths & PATH_NARROW_TRANSPOSE) != 0;
     if ((cfg.paths & ~PATH_NARROW_TRANSPOSE) == PATH_TRANSPOSE)
         return narrow ? launch_u<THREADS, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)
