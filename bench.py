@@ -20,9 +20,11 @@ reference library itself where it was built for this host, else the
 project's CPU restatement of it) on the same workload and prints the same
 line with "impl": "reference".
 
-Multi-GPU: the transform does not shard across GPUs here (no cross-GPU
-exchange is built): each rank runs an independent replica, `value` is the sum
-over ranks, timing is max over ranks ("scaling": "weak").
+Multi-GPU: `--gpus N` runs an independent replica per rank, `value` is the
+sum over ranks, timing is max over ranks ("scaling": "weak"). The sharded
+transform (virtual ranks spread over GPUs, grid2grid_gb300/exchange.py) is
+timed as `sharded_loopback`: two shards on one GPU, pack, buffer exchange
+and unpack.
 """
 from __future__ import annotations
 
@@ -412,6 +414,12 @@ def run_ours(args):
                 configs[name] = run_config_leg(lib, name, dev, stream, peak,
                                                max(args.steps, 20),
                                                cpu_reps=args.cpu_reps if ws == 1 else 0)
+        # the headline's layouts with op 'T' (float transposes: the staged
+        # ring of 4-byte transposed tiles), default tuning, no CPU leg
+        if w.name != "transposed_random_grid_f32_16384":
+            configs["transposed_random_grid_f32_16384"] = run_config_leg(
+                lib, "transposed_random_grid_f32_16384", dev, stream, peak,
+                max(args.steps, 20))
 
     sharded = None
     if args.batch and rank == 0 and w.ops is None and len(w.inits) == 1:
