@@ -516,7 +516,8 @@ void assemble(g2g_plan &pl) {
     pl.any_trans = false;
     pl.max_trans_esz = 0;
     pl.paths = 0;
-    bool only_w4 = true; // every CTA-level tile a plain transpose of 4-byte elements
+    // every CTA-level tile a plain transpose of 4-byte (8-byte) elements
+    bool only_w4 = true, only_w8 = true;
     for (int k = 0; k < pl.n_pairs; ++k) {
         PairHost &p = pl.host[k];
         g2g::PairInfo &pi = pl.pinfo[k];
@@ -605,9 +606,13 @@ void assemble(g2g_plan &pl) {
                         (p.any_trans && p.esz <= 8 ? 32 : 0);
         if (p.cast || p.scaled || (p.any_trans && p.esz != 4))
             only_w4 = false;
+        if (p.cast || p.scaled || (p.any_trans && p.esz != 8))
+            only_w8 = false;
     }
     if (only_w4 && (pl.paths & 2))
         pl.paths |= 64;
+    if (only_w8 && (pl.paths & 2))
+        pl.paths |= 128;
 }
 
 // Makes the device that holds the plan's blocks current for this library's
@@ -763,10 +768,11 @@ g2g_status plan_on_device(g2g_plan &pl) {
 // Largest dynamic shared memory a CTA can opt into on sm_100-class GPUs.
 constexpr size_t kMaxSmemPerCta = 227 * 1024;
 
-// A launch runs the staged ring of 4-byte transposes when those are its
-// only tiles (bit 64 set, no copy tiles).
-bool uses_w4_ring(int paths) {
-    return (paths & 64) && (paths & ~(64 | 32)) == 2;
+// A launch runs the staged ring of 4- or 8-byte transposes when those, of
+// one element size, are its only tiles (bit 64 or 128 set, no copy tiles).
+bool uses_staged_ring(int paths) {
+    return ((paths & ~(64 | 32)) == 2 && (paths & 64)) ||
+           ((paths & ~(128 | 32)) == 2 && (paths & 128));
 }
 
 g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
@@ -784,8 +790,8 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
                                     : 0;
     c.trans_bytes = c.smem_bytes;
     c.paths = pl.paths ? pl.paths : 1;
-    if (uses_w4_ring(c.paths)) // 4-byte transposes only: their staged ring
-        c.smem_bytes = g2g::staged_transpose_w4_smem_bytes(c.tile_dim);
+    if (uses_staged_ring(c.paths)) // narrow transposes only: their staged ring
+        c.smem_bytes = g2g::staged_transpose_smem_bytes(c.tile_dim);
     // blocks in host memory take the register path: plain loads and stores
     c.ring = (pl.tuning.ring == 1 && !pl.host_memory) ? 1 : 0;
     c.run_shift = 0;
@@ -840,8 +846,9 @@ cudaError_t launch_list(const g2g::PlanList &l, const g2g::ScatterConfig &cfg, c
 g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
     g2g::ScatterConfig c = scatter_config(*plans[0]);
     long long tiles = 0;
-    // bit 64 holds for the launch when every plan with CTA-level tiles has it
-    bool w4 = true;
+    // bit 64 (128) holds for the launch when every plan with CTA-level tiles
+    // has it
+    bool w4 = true, w8 = true;
     for (int k = 0; k < n; ++k) {
         const g2g::ScatterConfig ck = scatter_config(*plans[k]);
         if (plans[k]->host_memory) {
@@ -850,14 +857,16 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
         }
         if ((ck.paths & (2 | 4 | 8 | 16)) && !(ck.paths & 64))
             w4 = false;
+        if ((ck.paths & (2 | 4 | 8 | 16)) && !(ck.paths & 128))
+            w8 = false;
         c.paths |= ck.paths;
         c.trans_bytes = std::max(c.trans_bytes, ck.trans_bytes);
         tiles += plans[k]->n_tiles;
     }
-    c.paths = (c.paths & ~64) | (w4 && (c.paths & 2) ? 64 : 0);
-    c.smem_bytes = uses_w4_ring(c.paths)
-                       ? g2g::staged_transpose_w4_smem_bytes(c.tile_dim)
-                       : c.trans_bytes;
+    c.paths = (c.paths & ~(64 | 128)) | (w4 && (c.paths & 2) ? 64 : 0) |
+              (w8 && (c.paths & 2) ? 128 : 0);
+    c.smem_bytes = uses_staged_ring(c.paths) ? g2g::staged_transpose_smem_bytes(c.tile_dim)
+                                             : c.trans_bytes;
     if (c.stages >= 2) {
         while (c.stages >= 2 &&
                128 + (size_t)c.stages * c.stage_bytes + c.trans_bytes > kMaxSmemPerCta)

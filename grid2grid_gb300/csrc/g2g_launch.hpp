@@ -66,8 +66,8 @@ struct ScatterConfig {
     size_t smem_bytes = 0;   // dynamic shared memory (transposed tiles)
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled real,
                              // 8 scaled complex, 16 cast, 32 transposes of 4- or
-                             // 8-byte elements, 64 transposes of 4-byte elements
-                             // as the only CTA-level tiles
+                             // 8-byte elements, 64 / 128 transposes of 4- / 8-byte
+                             // elements as the only CTA-level tiles
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
     int ring = 0;            // plain copies through the per-warp cp.async ring
     int run_shift = 0;       // ring: runs of 2^run_shift consecutive tiles per warp
@@ -107,10 +107,10 @@ cudaError_t launch_scatter_512_elem(const PlanList &list, const ScatterConfig &c
 // whose edge is twice `tile_dim`).
 size_t transpose_smem_bytes(int tile_dim, int esz);
 
-// Shared memory of the staged ring of plain transposed tiles of 4-byte
-// elements (tile paths with bit 64: those tiles are a launch's only
-// CTA-level tiles).
-size_t staged_transpose_w4_smem_bytes(int tile_dim);
+// Shared memory of the staged ring of plain transposed tiles of 4- or 8-byte
+// elements (tile paths with bit 64 or 128: those tiles, of one element size,
+// are a launch's only tiles).
+size_t staged_transpose_smem_bytes(int tile_dim);
 
 // Launches the gather-scatter over the plans of `list`.
 cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,

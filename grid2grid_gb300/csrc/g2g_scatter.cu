@@ -54,8 +54,8 @@ size_t transpose_smem_bytes(int tile_dim, int esz) {
     return own > m ? own : m;
 }
 
-size_t staged_transpose_w4_smem_bytes(int tile_dim) {
-    return w4_staged_smem_bytes(tile_dim);
+size_t staged_transpose_smem_bytes(int tile_dim) {
+    return staged_smem_bytes(tile_dim);
 }
 
 int stage_bytes_for(int tile_bytes) {
@@ -114,6 +114,7 @@ cudaError_t preload_scatter_kernels() {
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
                              PATH_COPY | PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W4_STAGED,
+                             PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W8_STAGED,
                              PATH_COPY | PATH_SCALED_REAL, PATH_COPY | PATH_SCALED_COMPLEX,
                              PATH_COPY | PATH_CAST};
     for (int threads : {256, 512})
@@ -129,8 +130,8 @@ cudaError_t preload_scatter_kernels() {
                     c.paths = paths;
                     c.tile_dim = 32;
                     c.trans_bytes = c.smem_bytes = transpose_smem_bytes(32, 16);
-                    if (paths & PATH_W4_STAGED)
-                        c.smem_bytes = w4_staged_smem_bytes(32);
+                    if (paths & (PATH_W4_STAGED | PATH_W8_STAGED))
+                        c.smem_bytes = staged_smem_bytes(32);
                     c.ring = mode == 1;
                     c.stages = mode >= 2 ? mode : 0;
                     c.stage_bytes = stage_bytes_for(16 * 1024);

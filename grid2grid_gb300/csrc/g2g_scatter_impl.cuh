@@ -61,8 +61,9 @@ enum : int {
     PATH_CAST = 16,          // tiles converting the element type
     PATH_NARROW_TRANSPOSE = 32, // plain transposed tiles of 4- or 8-byte elements
                                 // (the wide and tall tile shapes)
-    PATH_W4_STAGED = 64 // every CTA-level tile a plain transpose of 4-byte
-                        // elements, staged raw through a cp.async ring
+    PATH_W4_STAGED = 64, // every CTA-level tile a plain transpose of 4-byte
+                         // elements, staged raw through a cp.async ring
+    PATH_W8_STAGED = 128 // the same for 8-byte elements
 };
 
 // ---------------------------------------------------------------- memory ops
@@ -1801,35 +1802,41 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
                                       : MinBlocks<U, THREADS>::value;
 };
 
-// Plain transposed tiles of 4-byte elements when they are the launch's only
-// CTA-level tiles (PATH_W4_STAGED): the tile's source lines are copied raw
-// into a ring of kW4Stages shared-memory stages with cp.async (the line's
-// 2 td / 4 aligned 16-byte blocks, one per lane, as the register path loads
-// them), so that a CTA keeps the next kW4Stages - 1 tiles in flight while it
-// stores the current one, without holding them in registers; the stores
+// Plain transposed tiles of one narrow element size when they are the
+// launch's only tiles (PATH_W4_STAGED: 4-byte elements, tiles of 2 td final
+// rows by 2 td - 4 columns; PATH_W8_STAGED: 8-byte elements, 2 td rows by td
+// columns): the tile's source lines are copied raw into a ring of kStages
+// shared-memory stages with cp.async (the line's aligned 16-byte blocks, one
+// per lane), so that a CTA keeps the next kStages - 1 tiles in flight while
+// it stores the current one, without holding them in registers; the stores
 // read each element at its line's phase. A stage is 2 td lines of 2 td + 4
-// words (16-byte aligned lines; a line's elements sit at words q .. q +
-// cols - 1, q its phase in words, and cols <= 2 td - 4).
-constexpr int kW4Stages = 3;
-template <int T> struct W4Stage {
+// words (16-byte aligned lines). A line of 4-byte elements (at most 2 td - 4
+// of them, 8 td - 16 bytes) lies at any phase in 2 td / 4 blocks, one of
+// 8-byte elements (at most td, 8 td bytes) in 2 td / 4 + 1; either way its
+// elements sit at words q .. q + cols * ES / 4 - 1 < 2 td + 4, q its phase
+// in words.
+constexpr int kStages = 3;
+template <int T> struct StagedTile {
     static constexpr int pitch = T + 4; // words per line
     static constexpr int bytes = T * pitch * 4;
 };
-__host__ __device__ constexpr size_t w4_staged_smem_bytes(int td) {
-    return (size_t)kW4Stages * (size_t)(2 * td) * (size_t)(2 * td + 4) * 4u;
+__host__ __device__ constexpr size_t staged_smem_bytes(int td) {
+    return (size_t)kStages * (size_t)(2 * td) * (size_t)(2 * td + 4) * 4u;
 }
 // Issues the copies of tile t's source lines into the stage at shared
 // address st (one 16-byte block per lane and pass; blocks past the line's
 // last element and lines past t.rows are not copied).
-template <int THREADS, int T>
-__device__ __forceinline__ void w4_issue(const Tile &t, uint32_t st) {
-    constexpr int G = T / 4;                          // lanes (blocks) per line
+template <int THREADS, int T, int ES>
+__device__ __forceinline__ void staged_issue(const Tile &t, uint32_t st) {
+    constexpr int G = ES == 4 ? T / 4 : T / 4 + 1;    // lanes (blocks) per line
     constexpr int RSTEP = THREADS / G;                // lines per pass
     constexpr int NP = (T + RSTEP - 1) / RSTEP;       // passes
-    constexpr int P = W4Stage<T>::pitch;
+    constexpr int P = StagedTile<T>::pitch;
     const int g = threadIdx.x % G;
     const int r0 = threadIdx.x / G;
-    const int run = t.cols * 4;
+    if (r0 >= RSTEP) // threads past the last whole line group
+        return;
+    const int run = t.cols * ES;
     const int rel = g * 16;
     uint64_t s = t.src + (uint64_t)((long long)r0 * t.src_ld);
     const uint64_t sstep = (uint64_t)((long long)RSTEP * t.src_ld);
@@ -1844,24 +1851,43 @@ __device__ __forceinline__ void w4_issue(const Tile &t, uint32_t st) {
     }
 }
 // Stores tile t from its stage: a thread per final row (source line) r,
-// columns c0, c0 + CSTEP, ...; element c of line r is word q_r + c.
-template <int THREADS, int T>
-__device__ __forceinline__ void w4_store(const Tile &t, const uint32_t *st) {
+// columns c0, c0 + CSTEP, ...; element c of line r starts at word
+// q_r + c * ES / 4. AL8: 8-byte elements whose source and destination
+// addresses and strides are all multiples of 8 (one 8-byte shared-memory
+// read and one 8-byte store per element; else two of 4 bytes).
+template <int THREADS, int T, int ES, bool AL8>
+__device__ __forceinline__ void staged_store(const Tile &t, const uint32_t *st) {
     constexpr int CSTEP = THREADS / T;
-    constexpr int NC = (T - 4 + CSTEP - 1) / CSTEP;
-    constexpr int P = W4Stage<T>::pitch;
+    constexpr int CMAX = ES == 4 ? T - 4 : T / 2;
+    constexpr int NC = (CMAX + CSTEP - 1) / CSTEP;
+    constexpr int P = StagedTile<T>::pitch;
+    constexpr int EW = ES / 4; // words per element
     const int r = threadIdx.x % T;
     const int c0 = threadIdx.x / T;
     if (r >= t.rows)
         return;
     const uint64_t s = t.src + (uint64_t)((long long)r * t.src_ld);
-    const uint32_t *p = st + r * P + (int)((s & 15u) >> 2) + c0;
-    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 4);
+    const uint32_t *p = st + r * P + (int)((s & 15u) >> 2) + c0 * EW;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ES);
     const uint64_t step = (uint64_t)((long long)CSTEP * t.dst_ld);
+    // complex<float> 'C': the imaginary part's sign is the top word's
+    const uint32_t flip = (ES == 8 && (t.kind & KIND_CONJ)) ? 0x80000000u : 0u;
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
-        if (c0 + i * CSTEP < t.cols)
-            st_u32(a, p[i * CSTEP]);
+        if (c0 + i * CSTEP < t.cols) {
+            const uint32_t *e = p + i * CSTEP * EW;
+            if constexpr (ES == 4) {
+                st_u32(a, e[0]);
+            } else if constexpr (AL8) {
+                const uint2 v = *reinterpret_cast<const uint2 *>(e);
+                asm volatile("st.global.v2.u32 [%0], {%1, %2};" ::"l"(a), "r"(v.x),
+                             "r"(v.y ^ flip)
+                             : "memory");
+            } else {
+                st_u32(a, e[0]);
+                st_u32(a + 4, e[1] ^ flip);
+            }
+        }
         a += step;
     }
 }
@@ -1871,11 +1897,11 @@ __device__ __forceinline__ void w4_store(const Tile &t, const uint32_t *st) {
 // thread has stored tile k - 1), refills stage (k - 1) % S with tile
 // k + S - 1 and stores tile k. Every step commits one copy group (empty
 // when no tile is left), so the wait always counts S - 2 younger groups.
-template <int THREADS, int TDS>
-__device__ __forceinline__ void cta_phase_w4(const PlanList &list, unsigned char *smem) {
+template <int THREADS, int TDS, int ES>
+__device__ __forceinline__ void cta_phase_staged(const PlanList &list, unsigned char *smem) {
     constexpr int T = 2 << TDS; // 2 td lines per tile
-    constexpr int S = kW4Stages;
-    constexpr int SB = W4Stage<T>::bytes;
+    constexpr int S = kStages;
+    constexpr int SB = StagedTile<T>::bytes;
     const long long n = list.total_cta;
     const long long G = gridDim.x;
     const uint32_t base = smem_addr(smem);
@@ -1884,7 +1910,8 @@ __device__ __forceinline__ void cta_phase_w4(const PlanList &list, unsigned char
     for (int k = 0; k < S - 1; ++k) {
         const long long ti = (long long)blockIdx.x + (long long)k * G;
         if (ti < n)
-            w4_issue<THREADS, T>(*locate_cta(list, ti, unused), base + (uint32_t)(k * SB));
+            staged_issue<THREADS, T, ES>(*locate_cta(list, ti, unused),
+                                         base + (uint32_t)(k * SB));
         cp_async_commit();
     }
     int st = 0;
@@ -1894,10 +1921,15 @@ __device__ __forceinline__ void cta_phase_w4(const PlanList &list, unsigned char
         const long long nx = ti + (long long)(S - 1) * G;
         const int sn = st == 0 ? S - 1 : st - 1;
         if (nx < n)
-            w4_issue<THREADS, T>(*locate_cta(list, nx, unused), base + (uint32_t)(sn * SB));
+            staged_issue<THREADS, T, ES>(*locate_cta(list, nx, unused),
+                                         base + (uint32_t)(sn * SB));
         cp_async_commit();
-        w4_store<THREADS, T>(*locate_cta(list, ti, unused),
-                             reinterpret_cast<const uint32_t *>(smem + st * SB));
+        const Tile t = *locate_cta(list, ti, unused);
+        const uint32_t *stage = reinterpret_cast<const uint32_t *>(smem + st * SB);
+        if (ES == 8 && elem_mode(t) == EM_8)
+            staged_store<THREADS, T, ES, true>(t, stage);
+        else
+            staged_store<THREADS, T, ES, false>(t, stage);
         st = st + 1 == S ? 0 : st + 1;
     }
     cp_async_wait<0>();
@@ -1911,7 +1943,11 @@ __device__ __forceinline__ void cta_phase_w4(const PlanList &list, unsigned char
 template <int THREADS, int PATHS, int TDS>
 __device__ __forceinline__ void cta_phase_t(const PlanList &list, unsigned char *smem) {
     if constexpr ((PATHS & PATH_W4_STAGED) != 0) {
-        cta_phase_w4<THREADS, TDS>(list, smem);
+        cta_phase_staged<THREADS, TDS, 4>(list, smem);
+        return;
+    }
+    if constexpr ((PATHS & PATH_W8_STAGED) != 0) {
+        cta_phase_staged<THREADS, TDS, 8>(list, smem);
         return;
     }
     constexpr int td = 1 << TDS;
@@ -2881,11 +2917,15 @@ template <int THREADS>
 cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
     if (cfg.paths == PATH_COPY)
         return launch_u<THREADS, PATH_COPY>(l, cfg, s);
-    // transposes of 4-byte elements only: the staged ring (no copy tiles, so
-    // the unroll knob has nothing to act on)
-    if ((cfg.paths & PATH_W4_STAGED) &&
-        (cfg.paths & ~(PATH_W4_STAGED | PATH_NARROW_TRANSPOSE)) == PATH_TRANSPOSE)
+    // transposes of 4- or 8-byte elements only: the staged ring (no copy
+    // tiles, so the unroll knob has nothing to act on)
+    if ((cfg.paths & ~(PATH_W4_STAGED | PATH_NARROW_TRANSPOSE)) == PATH_TRANSPOSE &&
+        (cfg.paths & PATH_W4_STAGED))
         return launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W4_STAGED>(
+            l, cfg, s);
+    if ((cfg.paths & ~(PATH_W8_STAGED | PATH_NARROW_TRANSPOSE)) == PATH_TRANSPOSE &&
+        (cfg.paths & PATH_W8_STAGED))
+        return launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W8_STAGED>(
             l, cfg, s);
     const bool narrow = (cfg.paths & PATH_NARROW_TRANSPOSE) != 0;
     if ((cfg.paths & ~PATH_NARROW_TRANSPOSE) == PATH_TRANSPOSE)

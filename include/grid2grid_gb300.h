@@ -166,10 +166,10 @@ typedef struct g2g_plan_info {
     int32_t tensor_boxes_ok;  /* 1 if the plan qualifies for tensor_boxes    */
     int32_t tile_paths;       /* tile kinds of the work list: 1 copy, 2 transpose,
                                  4 scaled real, 8 scaled complex, 16 cast,
-                                 32 transposes of 4- or 8-byte elements, 64
-                                 transposes of 4-byte elements only (they run
-                                 on the staged cp.async ring when no copy
-                                 tiles come with them)                        */
+                                 32 transposes of 4- or 8-byte elements,
+                                 64 / 128 transposes of 4- / 8-byte elements
+                                 only (they run on the staged cp.async ring
+                                 when no copy tiles come with them)           */
     g2g_tuning tuning;        /* knobs in effect                             */
 } g2g_plan_info;
 

@@ -1,9 +1,11 @@
-"""Plain transposes of 4-byte elements as a launch's only tiles (tile path
-64): their source lines are staged raw through a ring of shared-memory stages
-with cp.async and stored at each line's phase. Results must equal the oracle
-port's bit for bit, padding included, under every tile edge and CTA size, for
-plans, graphs, one-shot calls, batches and multi-plan launches; plans that
-mix them with other tiles keep the other kernels and stay exact too."""
+"""Plain transposes of one narrow element size as a launch's only tiles (tile
+path 64: float; 128: double and complex<float>): their source lines are
+staged raw through a ring of shared-memory stages with cp.async and stored
+at each line's phase. Results must equal the oracle port's bit for bit,
+padding included, under every tile edge and CTA size, for plans, graphs,
+one-shot calls, batches and multi-plan launches, at 8- and 4-byte aligned
+addresses; plans that mix them with other tiles keep the other kernels and
+stay exact too."""
 import ctypes as C
 
 import numpy as np
@@ -17,11 +19,12 @@ from grid2grid_gb300 import layouts as Ls
 pytestmark = pytest.mark.gpu
 
 STAGED = 64
+STAGED8 = 128
 
 
-def _staged(paths):
-    """The launch runs the staged ring: bit 64 and no tiles but transposes."""
-    return bool(paths & STAGED) and (paths & ~(STAGED | 32)) == 2
+def _staged(paths, bit=STAGED):
+    """The launch runs the staged ring: its bit and no tiles but transposes."""
+    return bool(paths & bit) and (paths & ~(bit | 32)) == 2
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -52,9 +55,11 @@ def _tile_paths(inits, finals, ops):
     return info.tile_paths
 
 
-def _float_pair(rng, m, n, t, ext_hi=90, P=5, mis=(0, 0)):
-    Li = Ls.random_grid_layout(n, m, P, capi.FLOAT32, rng, ext_hi=ext_hi, base_misalign=mis[0])
-    Lf = Ls.random_grid_layout(m, n, P, capi.FLOAT32, rng, ext_hi=ext_hi, base_misalign=mis[1])
+def _float_pair(rng, m, n, t, ext_hi=90, P=5, mis=(0, 0), dt=capi.FLOAT32, byte_mis=(0, 0)):
+    Li = Ls.random_grid_layout(n, m, P, dt, rng, ext_hi=ext_hi, base_misalign=mis[0],
+                               byte_misalign=byte_mis[0])
+    Lf = Ls.random_grid_layout(m, n, P, dt, rng, ext_hi=ext_hi, base_misalign=mis[1],
+                               byte_misalign=byte_mis[1])
     ai = Ls.fill_random(np.zeros(Li.arena_bytes, np.uint8), rng)
     af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
     return Li, Lf, ai, af, (t, 1.0, 0.0)
@@ -167,3 +172,45 @@ def test_multi_plan_launch_staged_and_mixed():
         for (Li, Lf, ai, af, op), df in zip(group, outs):
             want = T.port_run([Li], [Lf], [ai], [af], [op])[0]
             T.assert_arenas_equal(df.cpu().numpy(), want, Lf, what=f"multi {len(group)}")
+
+
+@pytest.mark.parametrize("dt", [capi.FLOAT64, capi.COMPLEX64])
+@pytest.mark.parametrize("tuning", [None, dict(tile_dim=16), dict(threads=512)])
+def test_eight_byte_transposes_staged_match_port(dt, tuning):
+    """Double and complex<float> 'T' / 'C' on random grids (8-byte aligned:
+    one 8-byte read and store per element), then complex<float> blocks at
+    4-byte aligned addresses (two 4-byte halves per element)."""
+    rng = np.random.default_rng(990 + dt * 7 + (0 if tuning is None else len(str(tuning))))
+    cases = [("T", (433, 611), (0, 0)), ("C", (700, 389), (0, 0))]
+    if dt == capi.COMPLEX64:
+        cases += [("C", (301, 257), (4, 0)), ("T", (257, 301), (0, 4)), ("T", (199, 211), (4, 4))]
+    for t, (m, n), bm in cases:
+        Li, Lf, ai, af, op = _float_pair(rng, m, n, t, dt=dt, byte_mis=bm)
+        assert _staged(_tile_paths([Li], [Lf], [op]), STAGED8)
+        want = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+        for how in ("plan", "graph"):
+            got = T.gpu_run([Li], [Lf], [ai], [af], [op], how=how, tuning=tuning,
+                            executes=2)[0]
+            T.assert_arenas_equal(got, want, Lf, what=f"dt{dt} {t} {bm} {how} {tuning}")
+
+
+def test_eight_byte_batches_and_mixed():
+    """A batch of double and complex<float> transposes runs staged; a float
+    transpose among them takes it off the ring; results stay the port's."""
+    rng = np.random.default_rng(1010)
+    pairs = [_float_pair(rng, int(rng.integers(40, 400)), int(rng.integers(40, 400)),
+                         "TC"[k % 2], dt=(capi.FLOAT64, capi.COMPLEX64)[k % 2]) for k in range(4)]
+    Lis, Lfs, ais, afs, ops = map(list, zip(*pairs))
+    assert _staged(_tile_paths(Lis, Lfs, ops), STAGED8)
+    want = T.port_run(Lis, Lfs, ais, afs, ops)
+    got = T.gpu_run(Lis, Lfs, ais, afs, ops, how="plan")
+    for k in range(len(Lis)):
+        T.assert_arenas_equal(got[k], want[k], Lfs[k], what=f"pair {k}")
+    Li, Lf, ai, af, op = _float_pair(rng, 120, 90, "T")
+    Li2, Lf2, ai2, af2, ops2 = Lis + [Li], Lfs + [Lf], ais + [ai], afs + [af], ops + [op]
+    paths = _tile_paths(Li2, Lf2, ops2)
+    assert not _staged(paths, STAGED8) and not _staged(paths, STAGED)
+    want2 = T.port_run(Li2, Lf2, ai2, af2, ops2)
+    got2 = T.gpu_run(Li2, Lf2, ai2, af2, ops2, how="plan")
+    for k in range(len(Li2)):
+        T.assert_arenas_equal(got2[k], want2[k], Lf2[k], what=f"mixed pair {k}")
