@@ -414,12 +414,12 @@ def run_ours(args):
                 configs[name] = run_config_leg(lib, name, dev, stream, peak,
                                                max(args.steps, 20),
                                                cpu_reps=args.cpu_reps if ws == 1 else 0)
-        # the headline's layouts with op 'T' (float transposes: the staged
-        # ring of 4-byte transposed tiles), default tuning, no CPU leg
-        if w.name != "transposed_random_grid_f32_16384":
-            configs["transposed_random_grid_f32_16384"] = run_config_leg(
-                lib, "transposed_random_grid_f32_16384", dev, stream, peak,
-                max(args.steps, 20))
+        # the headline's layouts with op 'T' in float and double (the staged
+        # ring of 4- and 8-byte transposed tiles), default tuning, no CPU leg
+        for name in ("transposed_random_grid_f32_16384", "transposed_random_grid_f64_16384"):
+            if name != w.name:
+                configs[name] = run_config_leg(lib, name, dev, stream, peak,
+                                               max(args.steps, 20))
 
     sharded = None
     if args.batch and rank == 0 and w.ops is None and len(w.inits) == 1:

@@ -88,6 +88,19 @@ def transposed_random_grid_f32_16384(m: int = 16384, seed: int = 2024, P: int = 
                           "final": "random splits U[1,2048], random owners, padded strides"})
 
 
+def transposed_random_grid_f64_16384(m: int = 16384, seed: int = 2024, P: int = 16) -> Workload:
+    """The same random grids in double with op 'T' (the tall transposed tiles
+    of 8-byte elements)."""
+    rng = np.random.default_rng(seed)
+    Li = Ls.random_grid_layout(m, m, P, capi.FLOAT64, rng)
+    Lf = Ls.random_grid_layout(m, m, P, capi.FLOAT64, rng)
+    return Workload(f"transposed_random_grid_f64_{m}", [Li], [Lf], [("T", 1.0, 0.0)],
+                    meta={"m": m, "n": m, "dtype": "float64", "ranks": P, "seed": seed,
+                          "op": "T",
+                          "initial": "random splits U[1,2048], random owners, padded strides",
+                          "final": "random splits U[1,2048], random owners, padded strides"})
+
+
 def _factor_grid(P: int, rng) -> tuple[int, int]:
     divs = [d for d in range(1, P + 1) if P % d == 0]
     pr = int(rng.choice(divs))
@@ -193,6 +206,7 @@ BY_NAME = {
     "random_grid_f32_16384": random_grid_f32_16384,
     "transposed_c128_8192": transposed_c128_8192,
     "transposed_random_grid_f32_16384": transposed_random_grid_f32_16384,
+    "transposed_random_grid_f64_16384": transposed_random_grid_f64_16384,
     "uneven_batch_256": uneven_batch,
     "uneven_batch_64": lambda: uneven_batch(64),
 }
