@@ -790,7 +790,11 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
                                     : 0;
     c.trans_bytes = c.smem_bytes;
     c.paths = pl.paths ? pl.paths : 1;
-    if (uses_staged_ring(c.paths)) // narrow transposes only: their staged ring
+    // narrow transposes only: their staged ring, unless the tuning asks for
+    // the register path or blocks live in host memory
+    if (pl.tuning.ring == -1 || pl.host_memory)
+        c.paths &= ~(64 | 128);
+    if (uses_staged_ring(c.paths))
         c.smem_bytes = g2g::staged_transpose_smem_bytes(c.tile_dim);
     // blocks in host memory take the register path: plain loads and stores
     c.ring = (pl.tuning.ring == 1 && !pl.host_memory) ? 1 : 0;
@@ -1504,7 +1508,12 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
                                     for (int pf : prefetch_opts) {
                                         if (th * c > 2048)
                                             continue;
-                                        if ((sg != -1 || rg != 1) && !(plan->paths & 1))
+                                        // without copy tiles the stages are moot and
+                                        // the ring knob only picks the staged ring of
+                                        // narrow transposes or their register path
+                                        if (!(plan->paths & 1) &&
+                                            (sg != -1 ||
+                                             (rg != 1 && !(plan->paths & (64 | 128)))))
                                             continue;
                                         if (sg != -1 && rg != 1)
                                             continue;

@@ -136,7 +136,9 @@ typedef struct g2g_tuning {
                                  many shared-memory stages (0 = default)    */
     int32_t ring;             /* plain copies when not TMA-staged: 1 = per-warp
                                  cp.async ring in shared memory, -1 = loads
-                                 through registers (0 = default)            */
+                                 through registers (0 = default). Launches of
+                                 plain 4- or 8-byte transposes only: 1 = their
+                                 staged cp.async ring, -1 = the register path */
     int32_t tile_run;         /* ring: a warp takes runs of this many
                                  consecutive tiles (1, 2, 4 .. 64; 0 = default) */
     int32_t l2_prefetch;      /* ring: 1 = a warp entering a tile asks L2 for
@@ -169,7 +171,9 @@ typedef struct g2g_plan_info {
                                  32 transposes of 4- or 8-byte elements,
                                  64 / 128 transposes of 4- / 8-byte elements
                                  only (they run on the staged cp.async ring
-                                 when no copy tiles come with them)           */
+                                 when no copy tiles come with them, the
+                                 tuning's ring is not -1 and no block is in
+                                 host memory)                                 */
     g2g_tuning tuning;        /* knobs in effect                             */
 } g2g_plan_info;
 

@@ -2,7 +2,8 @@
 path 64: float; 128: double and complex<float>): their source lines are
 staged raw through a ring of shared-memory stages with cp.async and stored
 at each line's phase. Results must equal the oracle port's bit for bit,
-padding included, under every tile edge and CTA size, for plans, graphs,
+padding included, under every tile edge and CTA size (and on the register
+path that the tuning's ring = -1 selects instead), for plans, graphs,
 one-shot calls, batches and multi-plan launches, at 8- and 4-byte aligned
 addresses; plans that mix them with other tiles keep the other kernels and
 stay exact too."""
@@ -66,7 +67,7 @@ def _float_pair(rng, m, n, t, ext_hi=90, P=5, mis=(0, 0), dt=capi.FLOAT32, byte_
 
 
 TUNINGS = [None, dict(tile_dim=16), dict(threads=512), dict(tile_dim=16, threads=512),
-           dict(ctas_per_sm=1), dict(ctas_per_sm=2, threads=512)]
+           dict(ctas_per_sm=1), dict(ctas_per_sm=2, threads=512), dict(ring=-1)]
 
 
 @pytest.mark.parametrize("tuning", TUNINGS)
@@ -175,7 +176,7 @@ def test_multi_plan_launch_staged_and_mixed():
 
 
 @pytest.mark.parametrize("dt", [capi.FLOAT64, capi.COMPLEX64])
-@pytest.mark.parametrize("tuning", [None, dict(tile_dim=16), dict(threads=512)])
+@pytest.mark.parametrize("tuning", [None, dict(tile_dim=16), dict(threads=512), dict(ring=-1)])
 def test_eight_byte_transposes_staged_match_port(dt, tuning):
     """Double and complex<float> 'T' / 'C' on random grids (8-byte aligned:
     one 8-byte read and store per element), then complex<float> blocks at
