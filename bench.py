@@ -1003,8 +1003,10 @@ def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
       first call), D2H of the final layout's arena.
     pipelined (the reported value): the same per-step work on two streams
       with two arena sets, so step k+1's H2D overlaps step k's D2H on the
-      host link; each step runs g2g_plan_execute of its set's plan. Three
-      trials of `steps` steps; the median trial is reported.
+      host link; each step runs g2g_plan_execute of its set's plan. Five
+      trials of `steps` steps; the median trial is reported (the host link
+      is shared with other work on the node, and single trials have run
+      twice as long as their neighbours).
     The device copy of the final arena mirrors the host one (same padding
     bytes), so copying it back leaves the host padding unchanged."""
     import torch
@@ -1071,14 +1073,14 @@ def run_e2e(lib, w, dev_i, dev_f, steps, stream, ws):
         pipe_step(k)
     torch.cuda.synchronize()
     trials = []
-    for _ in range(3):  # the host link varies between runs: median of 3 trials
+    for _ in range(5):  # the host link varies between runs: median of 5 trials
         _barrier(ws)
         t0 = time.perf_counter()
         for k in range(steps):
             pipe_step(k)
         torch.cuda.synchronize()
         trials.append(_allreduce_max((time.perf_counter() - t0) / steps, ws))
-    t_pipe = sorted(trials)[1]
+    t_pipe = sorted(trials)[2]
     for p in plans:
         capi.check(lib.g2g_plan_destroy(p))
 
