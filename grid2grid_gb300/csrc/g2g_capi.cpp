@@ -516,8 +516,9 @@ void assemble(g2g_plan &pl) {
     pl.any_trans = false;
     pl.max_trans_esz = 0;
     pl.paths = 0;
-    // every CTA-level tile a plain transpose of 4-byte (8-byte) elements
-    bool only_w4 = true, only_w8 = true;
+    // every CTA-level tile a plain transpose of 4-byte (8-byte) elements;
+    // every tile a scaled transpose of 4-byte (8-byte) elements
+    bool only_w4 = true, only_w8 = true, only_w4s = true, only_w8s = true;
     for (int k = 0; k < pl.n_pairs; ++k) {
         PairHost &p = pl.host[k];
         g2g::PairInfo &pi = pl.pinfo[k];
@@ -608,11 +609,19 @@ void assemble(g2g_plan &pl) {
             only_w4 = false;
         if (p.cast || p.scaled || (p.any_trans && p.esz != 8))
             only_w8 = false;
+        if (!p.scaled || p.cast || any_plain || p.esz != 4)
+            only_w4s = false;
+        if (!p.scaled || p.cast || any_plain || p.esz != 8)
+            only_w8s = false;
     }
     if (only_w4 && (pl.paths & 2))
         pl.paths |= 64;
     if (only_w8 && (pl.paths & 2))
         pl.paths |= 128;
+    if (only_w4s && pl.n_pairs > 0)
+        pl.paths |= 1024;
+    if (only_w8s && pl.n_pairs > 0)
+        pl.paths |= 2048;
 }
 
 // Makes the device that holds the plan's blocks current for this library's
@@ -774,6 +783,11 @@ bool uses_staged_ring(int paths) {
     return ((paths & ~(64 | 32)) == 2 && (paths & 64)) ||
            ((paths & ~(128 | 32)) == 2 && (paths & 128));
 }
+// ... and the staged ring of scaled transposes when every tile is a scaled
+// transpose of one element size (bit 1024 or 2048 set).
+bool uses_staged_scaled_ring(int paths) {
+    return paths == (4 | 1024) || ((paths & 2048) && !(paths & ~(4 | 8 | 2048)));
+}
 
 g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     g2g::ScatterConfig c;
@@ -793,9 +807,11 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     // narrow transposes only: their staged ring, unless the tuning asks for
     // the register path or blocks live in host memory
     if (pl.tuning.ring == -1 || pl.host_memory)
-        c.paths &= ~(64 | 128);
+        c.paths &= ~(64 | 128 | 1024 | 2048);
     if (uses_staged_ring(c.paths))
         c.smem_bytes = g2g::staged_transpose_smem_bytes(c.tile_dim);
+    if (uses_staged_scaled_ring(c.paths))
+        c.smem_bytes = g2g::staged_scaled_transpose_smem_bytes(c.tile_dim);
     // blocks in host memory take the register path: plain loads and stores
     c.ring = (pl.tuning.ring == 1 && !pl.host_memory) ? 1 : 0;
     c.run_shift = 0;
@@ -851,8 +867,8 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
     g2g::ScatterConfig c = scatter_config(*plans[0]);
     long long tiles = 0;
     // bit 64 (128) holds for the launch when every plan with CTA-level tiles
-    // has it
-    bool w4 = true, w8 = true;
+    // has it, bit 1024 (2048) when every plan has it
+    bool w4 = true, w8 = true, w4s = true, w8s = true;
     for (int k = 0; k < n; ++k) {
         const g2g::ScatterConfig ck = scatter_config(*plans[k]);
         if (plans[k]->host_memory) {
@@ -863,14 +879,20 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
             w4 = false;
         if ((ck.paths & (2 | 4 | 8 | 16)) && !(ck.paths & 128))
             w8 = false;
+        if (!(ck.paths & 1024))
+            w4s = false;
+        if (!(ck.paths & 2048))
+            w8s = false;
         c.paths |= ck.paths;
         c.trans_bytes = std::max(c.trans_bytes, ck.trans_bytes);
         tiles += plans[k]->n_tiles;
     }
-    c.paths = (c.paths & ~(64 | 128)) | (w4 && (c.paths & 2) ? 64 : 0) |
-              (w8 && (c.paths & 2) ? 128 : 0);
+    c.paths = (c.paths & ~(64 | 128 | 1024 | 2048)) | (w4 && (c.paths & 2) ? 64 : 0) |
+              (w8 && (c.paths & 2) ? 128 : 0) | (w4s ? 1024 : 0) | (w8s ? 2048 : 0);
     c.smem_bytes = uses_staged_ring(c.paths) ? g2g::staged_transpose_smem_bytes(c.tile_dim)
-                                             : c.trans_bytes;
+                   : uses_staged_scaled_ring(c.paths)
+                       ? g2g::staged_scaled_transpose_smem_bytes(c.tile_dim)
+                       : c.trans_bytes;
     if (c.stages >= 2) {
         while (c.stages >= 2 &&
                128 + (size_t)c.stages * c.stage_bytes + c.trans_bytes > kMaxSmemPerCta)

@@ -67,7 +67,8 @@ struct ScatterConfig {
     int paths = 7;           // tile paths present: 1 copy, 2 transpose, 4 scaled real,
                              // 8 scaled complex, 16 cast, 32 transposes of 4- or
                              // 8-byte elements, 64 / 128 transposes of 4- / 8-byte
-                             // elements as the only CTA-level tiles
+                             // elements as the only CTA-level tiles, 1024 / 2048
+                             // scaled transposes of 4- / 8-byte elements only
     int stages = 0;          // TMA staging ring depth for plain copies (0 = none)
     int ring = 0;            // plain copies through the per-warp cp.async ring
     int run_shift = 0;       // ring: runs of 2^run_shift consecutive tiles per warp
@@ -111,6 +112,9 @@ size_t transpose_smem_bytes(int tile_dim, int esz);
 // elements (tile paths with bit 64 or 128: those tiles, of one element size,
 // are a launch's only tiles).
 size_t staged_transpose_smem_bytes(int tile_dim);
+// ... and of the staged ring of scaled transposed tiles (bits 1024 / 2048),
+// whose stages hold the destination columns too.
+size_t staged_scaled_transpose_smem_bytes(int tile_dim);
 
 // Launches the gather-scatter over the plans of `list`.
 cudaError_t launch_scatter(const PlanList &list, const ScatterConfig &cfg,

@@ -58,6 +58,10 @@ size_t staged_transpose_smem_bytes(int tile_dim) {
     return staged_smem_bytes(tile_dim);
 }
 
+size_t staged_scaled_transpose_smem_bytes(int tile_dim) {
+    return staged_scaled_smem_bytes(tile_dim);
+}
+
 int stage_bytes_for(int tile_bytes) {
     const long long b = (long long)tile_bytes * 9 / 8 + 512;
     return (int)((b + 127) / 128 * 128);
@@ -116,7 +120,8 @@ cudaError_t preload_scatter_kernels() {
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W4_STAGED,
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W8_STAGED,
                              PATH_COPY | PATH_SCALED_REAL, PATH_COPY | PATH_SCALED_COMPLEX,
-                             PATH_COPY | PATH_CAST};
+                             PATH_COPY | PATH_CAST, PATH_SCALED_REAL | PATH_W4S_STAGED,
+                             PATH_SCALED | PATH_W8S_STAGED};
     for (int threads : {256, 512})
         for (int unroll : {1, 2, 4})
             for (int paths : path_sets)
@@ -132,6 +137,8 @@ cudaError_t preload_scatter_kernels() {
                     c.trans_bytes = c.smem_bytes = transpose_smem_bytes(32, 16);
                     if (paths & (PATH_W4_STAGED | PATH_W8_STAGED))
                         c.smem_bytes = staged_smem_bytes(32);
+                    if (paths & (PATH_W4S_STAGED | PATH_W8S_STAGED))
+                        c.smem_bytes = staged_scaled_smem_bytes(32);
                     c.ring = mode == 1;
                     c.stages = mode >= 2 ? mode : 0;
                     c.stage_bytes = stage_bytes_for(16 * 1024);

@@ -63,7 +63,10 @@ enum : int {
                                 // (the wide and tall tile shapes)
     PATH_W4_STAGED = 64, // every CTA-level tile a plain transpose of 4-byte
                          // elements, staged raw through a cp.async ring
-    PATH_W8_STAGED = 128 // the same for 8-byte elements
+    PATH_W8_STAGED = 128, // the same for 8-byte elements
+    PATH_W4S_STAGED = 1024, // every tile a scaled transposed tile of 4-byte
+                            // elements: the ring stages their destination too
+    PATH_W8S_STAGED = 2048  // the same for 8-byte elements
 };
 
 // ---------------------------------------------------------------- memory ops
@@ -1935,6 +1938,150 @@ __device__ __forceinline__ void cta_phase_staged(const PlanList &list, unsigned 
     cp_async_wait<0>();
 }
 
+// Scaled transposed tiles of one element size (4 or 8 bytes) when they are
+// the launch's only tiles (PATH_W4S_STAGED, PATH_W8S_STAGED): the ring stages
+// the source lines as above and, behind them in the same stage, the tile's
+// destination columns (final rows are their contiguous direction): column c
+// at c * 4 GD words, GD = (2 td * ES + 27) / 16 blocks for a run of at most
+// 2 td elements at a phase of at most 12 bytes. The stores combine
+// beta * d + alpha * op(s) with both operands read from the stage, so no
+// destination load waits in the store loop.
+template <int TD, int ES> struct StagedDst {
+    static constexpr int lines = 2 * TD;                // final rows of a tile
+    static constexpr int cmax = ES == 4 ? 2 * TD - 4 : TD; // its columns at most
+    static constexpr int blocks = (lines * ES + 27) / 16;
+    static constexpr int pitch = 4 * blocks; // words per column
+    static constexpr int bytes = cmax * pitch * 4;
+};
+__host__ __device__ constexpr size_t staged_scaled_smem_bytes(int td) {
+    const size_t src = (size_t)(2 * td) * (size_t)(2 * td + 4) * 4u;
+    const size_t d4 = (size_t)(2 * td - 4) * 4u * (size_t)((2 * td * 4 + 27) / 16) * 4u;
+    const size_t d8 = (size_t)td * 4u * (size_t)((2 * td * 8 + 27) / 16) * 4u;
+    return (size_t)kStages * (src + (d4 > d8 ? d4 : d8));
+}
+template <int THREADS, int TD, int ES>
+__device__ __forceinline__ void staged_issue_dst(const Tile &t, uint32_t st) {
+    constexpr int GD = StagedDst<TD, ES>::blocks;
+    const int total = t.cols * GD;
+    const int run = t.rows * ES;
+    for (int f = threadIdx.x; f < total; f += THREADS) {
+        const int c = f / GD;
+        const int g = f - c * GD;
+        const uint64_t dc = t.dst + (uint64_t)((long long)c * t.dst_ld);
+        const int ph = (int)(dc & 15u);
+        if (g * 16 < ph + run)
+            cp_async16(st + (uint32_t)((c * GD + g) * 16), dc - (uint64_t)ph + (uint64_t)(g * 16));
+    }
+}
+template <int THREADS, int TD, int ES, typename T, int MODE, int CM>
+__device__ __forceinline__ void staged_store_scaled(const Tile &t, const uint32_t *ss,
+                                                    const uint32_t *sd, const Coef<T> &k) {
+    using SD = StagedDst<TD, ES>;
+    constexpr int TL = SD::lines;
+    constexpr int P = StagedTile<TL>::pitch;
+    constexpr int CSTEP = THREADS / TL;
+    constexpr int NC = (SD::cmax + CSTEP - 1) / CSTEP;
+    constexpr int EW = ES / 4;
+    const int r = threadIdx.x % TL;
+    const int c0 = threadIdx.x / TL;
+    if (r >= t.rows)
+        return;
+    const uint64_t s = t.src + (uint64_t)((long long)r * t.src_ld);
+    const uint32_t *ps = ss + r * P + (int)((s & 15u) >> 2) + c0 * EW;
+    const uint32_t *pd = sd + c0 * SD::pitch + r * EW;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * ES);
+    const uint64_t step = (uint64_t)((long long)CSTEP * t.dst_ld);
+    const uint32_t flip = (ES == 8 && (t.kind & KIND_CONJ)) ? 0x80000000u : 0u;
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        if (c0 + i * CSTEP < t.cols) {
+            const uint32_t *e = ps + i * CSTEP * EW;
+            // the column's phase: that of the element's address less its row
+            const int qd = (int)(((a - (uint64_t)(r * ES)) & 15u) >> 2);
+            const uint32_t *dw = pd + i * CSTEP * SD::pitch + qd;
+            uint4 sv = make_uint4(e[0], 0u, 0u, 0u), dv = make_uint4(dw[0], 0u, 0u, 0u);
+            if constexpr (EW == 2) {
+                sv.y = e[1] ^ flip;
+                dv.y = dw[1];
+            }
+            st_elem_raw(a, to_words(axpby_m<CM>(k, from_words<T>(sv), from_words<T>(dv))),
+                        MODE);
+        }
+        a += step;
+    }
+}
+template <int THREADS, int TD, int ES, typename T>
+__device__ __forceinline__ void staged_store_scaled_t(const Tile &t, const uint32_t *ss,
+                                                      const uint32_t *sd, const PairInfo *pairs) {
+    const Coef<T> k = coef_from<T>(pairs[t.pair]);
+    const bool al = ES == 4 || elem_mode(t) == EM_8;
+    coef_dispatch(k, [&](auto cm) {
+        constexpr int CM = decltype(cm)::value;
+        if (ES == 4)
+            staged_store_scaled<THREADS, TD, ES, T, EM_4, CM>(t, ss, sd, k);
+        else if (al)
+            staged_store_scaled<THREADS, TD, ES, T, EM_8, CM>(t, ss, sd, k);
+        else
+            staged_store_scaled<THREADS, TD, ES, T, EM_8_SPLIT, CM>(t, ss, sd, k);
+    });
+}
+// The ring of cta_phase_staged with each stage holding the source lines and
+// then the destination columns of its tile.
+template <int THREADS, int TDS, int ES, int PATHS>
+__device__ __forceinline__ void cta_phase_staged_scaled(const PlanList &list,
+                                                        unsigned char *smem) {
+    constexpr int TD = 1 << TDS;
+    constexpr int S = kStages;
+    constexpr int SBS = StagedTile<2 * TD>::bytes;
+    constexpr int SB = SBS + StagedDst<TD, ES>::bytes;
+    const long long n = list.total_cta;
+    const long long G = gridDim.x;
+    const uint32_t base = smem_addr(smem);
+    const PairInfo *unused;
+#pragma unroll
+    for (int k = 0; k < S - 1; ++k) {
+        const long long ti = (long long)blockIdx.x + (long long)k * G;
+        if (ti < n) {
+            const Tile t = *locate_cta(list, ti, unused);
+            staged_issue<THREADS, 2 * TD, ES>(t, base + (uint32_t)(k * SB));
+            staged_issue_dst<THREADS, TD, ES>(t, base + (uint32_t)(k * SB + SBS));
+        }
+        cp_async_commit();
+    }
+    int st = 0;
+    for (long long ti = blockIdx.x; ti < n; ti += G) {
+        cp_async_wait<S - 2>();
+        __syncthreads();
+        const long long nx = ti + (long long)(S - 1) * G;
+        const int sn = st == 0 ? S - 1 : st - 1;
+        if (nx < n) {
+            const Tile t = *locate_cta(list, nx, unused);
+            staged_issue<THREADS, 2 * TD, ES>(t, base + (uint32_t)(sn * SB));
+            staged_issue_dst<THREADS, TD, ES>(t, base + (uint32_t)(sn * SB + SBS));
+        }
+        cp_async_commit();
+        const PairInfo *pairs;
+        const Tile t = *locate_cta(list, ti, pairs);
+        const uint32_t *ss = reinterpret_cast<const uint32_t *>(smem + st * SB);
+        const uint32_t *sd = reinterpret_cast<const uint32_t *>(smem + st * SB + SBS);
+        if constexpr (ES == 4) {
+            staged_store_scaled_t<THREADS, TD, 4, float>(t, ss, sd, pairs);
+        } else {
+            const uint32_t dt = (t.kind >> KIND_DTYPE_SHIFT) & 3u;
+            if constexpr ((PATHS & PATH_SCALED_COMPLEX) != 0) {
+                if (dt == 2u) {
+                    staged_store_scaled_t<THREADS, TD, 8, cplxf>(t, ss, sd, pairs);
+                    st = st + 1 == S ? 0 : st + 1;
+                    continue;
+                }
+            }
+            staged_store_scaled_t<THREADS, TD, 8, double>(t, ss, sd, pairs);
+        }
+        st = st + 1 == S ? 0 : st + 1;
+    }
+    cp_async_wait<0>();
+}
+
 // CTA-level tiles (transposed, and scaled or cast ones that are not
 // warp-level) of a launch, static striding, with the next plain transposed
 // tile's loads issued before the current tile is stored.
@@ -1948,6 +2095,14 @@ __device__ __forceinline__ void cta_phase_t(const PlanList &list, unsigned char 
     }
     if constexpr ((PATHS & PATH_W8_STAGED) != 0) {
         cta_phase_staged<THREADS, TDS, 8>(list, smem);
+        return;
+    }
+    if constexpr ((PATHS & PATH_W4S_STAGED) != 0) {
+        cta_phase_staged_scaled<THREADS, TDS, 4, PATHS>(list, smem);
+        return;
+    }
+    if constexpr ((PATHS & PATH_W8S_STAGED) != 0) {
+        cta_phase_staged_scaled<THREADS, TDS, 8, PATHS>(list, smem);
         return;
     }
     constexpr int td = 1 << TDS;
@@ -2938,6 +3093,12 @@ cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cuda
 // Plans with element arithmetic: scaled or cast tiles (and any others).
 template <int THREADS>
 cudaError_t launch_elem_paths(const PlanList &l, const ScatterConfig &cfg, cudaStream_t s) {
+    // scaled transposes of one element size only: the staged ring (no copy
+    // tiles, so the unroll knob has nothing to act on)
+    if (cfg.paths == (PATH_SCALED_REAL | PATH_W4S_STAGED))
+        return launch_t<THREADS, 1, PATH_SCALED_REAL | PATH_W4S_STAGED>(l, cfg, s);
+    if ((cfg.paths & PATH_W8S_STAGED) && !(cfg.paths & ~(PATH_SCALED | PATH_W8S_STAGED)))
+        return launch_t<THREADS, 1, PATH_SCALED | PATH_W8S_STAGED>(l, cfg, s);
     if (cfg.paths & PATH_CAST) {
         if (cfg.paths & PATH_SCALED) // not generated: cast and scaled plans launch apart
             return cudaErrorNotSupported;

@@ -173,7 +173,9 @@ typedef struct g2g_plan_info {
                                  only (they run on the staged cp.async ring
                                  when no copy tiles come with them, the
                                  tuning's ring is not -1 and no block is in
-                                 host memory)                                 */
+                                 host memory), 1024 / 2048 scaled transposes
+                                 of 4- / 8-byte elements only (their staged
+                                 ring, on the same conditions)                */
     g2g_tuning tuning;        /* knobs in effect                             */
 } g2g_plan_info;
 

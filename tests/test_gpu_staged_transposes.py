@@ -1,7 +1,8 @@
 """Plain transposes of one narrow element size as a launch's only tiles (tile
-path 64: float; 128: double and complex<float>): their source lines are
-staged raw through a ring of shared-memory stages with cp.async and stored
-at each line's phase. Results must equal the oracle port's bit for bit,
+path 64: float; 128: double and complex<float>), and scaled ones (1024,
+2048): their source lines (and for scaled tiles the destination columns)
+are staged raw through a ring of shared-memory stages with cp.async and
+stored at each line's phase. Results must equal the oracle port's bit for bit,
 padding included, under every tile edge and CTA size (and on the register
 path that the tuning's ring = -1 selects instead), for plans, graphs,
 one-shot calls, batches and multi-plan launches, at 8- and 4-byte aligned
@@ -215,3 +216,73 @@ def test_eight_byte_batches_and_mixed():
     got2 = T.gpu_run(Li2, Lf2, ai2, af2, ops2, how="plan")
     for k in range(len(Li2)):
         T.assert_arenas_equal(got2[k], want2[k], Lf2[k], what=f"mixed pair {k}")
+
+
+STAGED_SC4, STAGED_SC8 = 1024, 2048
+
+
+def _scaled_staged(paths, bit):
+    return bool(paths & bit) and not (paths & ~(4 | 8 | bit))
+
+
+def _normal_arena(rng, L, dt):
+    comp = np.float32 if dt in (capi.FLOAT32, capi.COMPLEX64) else np.float64
+    return np.frombuffer(rng.standard_normal(L.arena_bytes // np.dtype(comp).itemsize)
+                         .astype(comp).tobytes(), np.uint8).copy()
+
+
+@pytest.mark.parametrize("dt", [capi.FLOAT32, capi.FLOAT64, capi.COMPLEX64])
+@pytest.mark.parametrize("tuning", [None, dict(tile_dim=16), dict(threads=512), dict(ring=-1)])
+def test_scaled_transposes_staged_match_port(dt, tuning):
+    """final = beta * final + alpha * op(initial) with every tile a scaled
+    transpose of one element size (tile paths 1024 / 2048): source lines and
+    destination columns staged; 'T' and 'C', several coefficient forms,
+    4-byte aligned complex<float> blocks; finite values, bit for bit."""
+    rng = np.random.default_rng(1200 + dt * 5 + (0 if tuning is None else len(str(tuning))))
+    bit = STAGED_SC4 if dt == capi.FLOAT32 else STAGED_SC8
+    coefs = [(2.0, 0.5), (1.0, 1.0), (-0.75, 0.0), (0.5, -1.5)]
+    cases = [("T", (433, 301), (0, 0)), ("C", (280, 377), (0, 0))]
+    if dt == capi.COMPLEX64:
+        cases.append(("C", (211, 173), (4, 4)))
+    for k, (t, (m, n), bm) in enumerate(cases):
+        Li, Lf, _, _, _ = _float_pair(rng, m, n, t, dt=dt, byte_mis=bm, ext_hi=120)
+        ai, af = _normal_arena(rng, Li, dt), _normal_arena(rng, Lf, dt)
+        a, b = coefs[k % len(coefs)]
+        op = (t, a, b)
+        assert _scaled_staged(_tile_paths([Li], [Lf], [op]), bit)
+        want = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+        for how in ("plan", "graph"):
+            got = T.gpu_run([Li], [Lf], [ai], [af], [op], how=how, tuning=tuning, executes=1)[0]
+            T.assert_arenas_equal(got, want, Lf, what=f"scaled dt{dt} {op} {bm} {how} {tuning}")
+
+
+def test_scaled_transposes_batch_and_mixed():
+    """A batch of scaled double and complex<float> transposes runs staged;
+    with a plain transpose or a scaled copy among them it does not; results
+    stay the port's."""
+    rng = np.random.default_rng(1300)
+    pairs, ops = [], []
+    for k in range(4):
+        dt = (capi.FLOAT64, capi.COMPLEX64)[k % 2]
+        Li, Lf, _, _, _ = _float_pair(rng, int(rng.integers(50, 300)), int(rng.integers(50, 300)),
+                                      "TC"[k % 2], dt=dt, ext_hi=100)
+        pairs.append((Li, Lf, _normal_arena(rng, Li, dt), _normal_arena(rng, Lf, dt)))
+        ops.append(("TC"[k % 2], 1.5, -0.25))
+    Lis, Lfs, ais, afs = map(list, zip(*pairs))
+    assert _scaled_staged(_tile_paths(Lis, Lfs, ops), STAGED_SC8)
+    want = T.port_run(Lis, Lfs, ais, afs, ops)
+    got = T.gpu_run(Lis, Lfs, ais, afs, ops, how="plan")
+    for k in range(len(Lis)):
+        T.assert_arenas_equal(got[k], want[k], Lfs[k], what=f"scaled batch pair {k}")
+    Lx, Ly, _, _, _ = _float_pair(rng, 120, 90, "T", dt=capi.FLOAT64)
+    Lc_i = Ls.random_grid_layout(110, 95, 4, capi.FLOAT64, rng, ext_hi=40)
+    Lc_f = Ls.random_grid_layout(110, 95, 4, capi.FLOAT64, rng, ext_hi=40)
+    for Li, Lf, op in ((Lx, Ly, ("T", 1.0, 0.0)), (Lc_i, Lc_f, ("N", 2.0, 0.5))):
+        Li2, Lf2, ops2 = Lis + [Li], Lfs + [Lf], ops + [op]
+        ai2 = ais + [_normal_arena(rng, Li, capi.FLOAT64)]
+        af2 = afs + [_normal_arena(rng, Lf, capi.FLOAT64)]
+        assert not _scaled_staged(_tile_paths(Li2, Lf2, ops2), STAGED_SC8)
+        want2 = T.port_run(Li2, Lf2, ai2, af2, ops2)
+        got2 = T.gpu_run(Li2, Lf2, ai2, af2, ops2, how="plan")
+        for k in range(len(Li2)):
+            T.assert_arenas_equal(got2[k], want2[k], Lf2[k], what=f"scaled mixed pair {k}")
