@@ -420,6 +420,11 @@ def run_ours(args):
             if name != w.name:
                 configs[name] = run_config_leg(lib, name, dev, stream, peak,
                                                max(args.steps, 20))
+        # float 'T' with alpha = 2, beta = 0.5 (the staged ring of scaled
+        # transposes: 3x the traffic)
+        configs["transposed_random_grid_f32_16384_scaled"] = run_config_leg(
+            lib, "transposed_random_grid_f32_16384", dev, stream, peak, max(args.steps, 20),
+            ops=[("T", 2.0, 0.5)])
 
     sharded = None
     if args.batch and rank == 0 and w.ops is None and len(w.inits) == 1:
@@ -529,7 +534,7 @@ def _time_steps(stream, fn, steps, warmup):
     return a.elapsed_time(b) / steps
 
 
-def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
+def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0, ops=None):
     """One single-transform configuration, device-resident, plan cached, one
     launch per step timed with CUDA events on the launching stream. Inputs
     smaller than L2 get it flushed before every step, outside the events (a
@@ -540,6 +545,8 @@ def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
     from grid2grid_gb300 import capi
     from grid2grid_gb300 import workloads as W
     w = W.BY_NAME[name]()
+    if ops is not None:  # the workload's layouts under other ops (alpha, beta)
+        w = W.Workload(w.name + "_scaled", w.inits, w.finals, ops, meta=dict(w.meta or {}))
     di, df = _device_arenas(w, dev, 4321)
     keep = []
     n = len(w.inits)
@@ -607,7 +614,7 @@ def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
                "kind": kind, "sample": sample}
     del di, df, flush, flush_rd
     torch.cuda.empty_cache()
-    return {"workload": name, "config": dict(w.meta), "ms_per_step": round(ms, 5),
+    return {"workload": w.name, "config": dict(w.meta, ops=w.ops), "ms_per_step": round(ms, 5),
             "cpu_baseline": cpu, "tensor_boxes": boxes,
             "value": round(w.bytes_moved / (ms * 1e-3) / 1e9, 2), "unit": UNIT,
             "steps": steps, "pieces": info.n_pieces, "tiles": info.n_tiles,
@@ -615,7 +622,7 @@ def run_config_leg(lib, name, dev, stream, peak, steps, cpu_reps=0):
                   else "inputs larger than L2 (no flush)",
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
-                         "traffic": _profile_traffic("g2g_scatter", name),
+                         "traffic": _profile_traffic("g2g_scatter", w.name),
                          "algorithmic_bytes_per_launch": info.bytes_min_traffic}}
 
 

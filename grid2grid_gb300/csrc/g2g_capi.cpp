@@ -1535,7 +1535,8 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
                                         // narrow transposes or their register path
                                         if (!(plan->paths & 1) &&
                                             (sg != -1 ||
-                                             (rg != 1 && !(plan->paths & (64 | 128)))))
+                                             (rg != 1 &&
+                                              !(plan->paths & (64 | 128 | 1024 | 2048)))))
                                             continue;
                                         if (sg != -1 && rg != 1)
                                             continue;
