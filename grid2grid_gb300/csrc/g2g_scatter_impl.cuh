@@ -1818,7 +1818,10 @@ template <int PATHS, int U, int THREADS> struct MinBlocksP {
 // 8-byte elements (at most td, 8 td bytes) in 2 td / 4 + 1; either way its
 // elements sit at words q .. q + cols * ES / 4 - 1 < 2 td + 4, q its phase
 // in words.
-constexpr int kStages = 3;
+// Two stages: more CTAs per SM (shared memory is what limits them) beat a
+// deeper ring (float 'T' on random grids 16384² 0.410 -> 0.395 ms with two
+// stages instead of three, block-cyclic 64x64 -> 96x200 0.637 -> 0.542 ms).
+constexpr int kStages = 2;
 template <int T> struct StagedTile {
     static constexpr int pitch = T + 4; // words per line
     static constexpr int bytes = T * pitch * 4;
@@ -1953,11 +1956,15 @@ template <int TD, int ES> struct StagedDst {
     static constexpr int pitch = 4 * blocks; // words per column
     static constexpr int bytes = cmax * pitch * 4;
 };
+// Two stages as well (a stage is twice the plain ring's): three CTAs of two
+// stages per SM outran two CTAs of three (float 'T' with α/β on random grids
+// 16384² 0.748 -> 0.606 ms).
+constexpr int kScaledStages = 2;
 __host__ __device__ constexpr size_t staged_scaled_smem_bytes(int td) {
     const size_t src = (size_t)(2 * td) * (size_t)(2 * td + 4) * 4u;
     const size_t d4 = (size_t)(2 * td - 4) * 4u * (size_t)((2 * td * 4 + 27) / 16) * 4u;
     const size_t d8 = (size_t)td * 4u * (size_t)((2 * td * 8 + 27) / 16) * 4u;
-    return (size_t)kStages * (src + (d4 > d8 ? d4 : d8));
+    return (size_t)kScaledStages * (src + (d4 > d8 ? d4 : d8));
 }
 template <int THREADS, int TD, int ES>
 __device__ __forceinline__ void staged_issue_dst(const Tile &t, uint32_t st) {
@@ -2025,13 +2032,14 @@ __device__ __forceinline__ void staged_store_scaled_t(const Tile &t, const uint3
             staged_store_scaled<THREADS, TD, ES, T, EM_8_SPLIT, CM>(t, ss, sd, k);
     });
 }
-// The ring of cta_phase_staged with each stage holding the source lines and
-// then the destination columns of its tile.
+// The ring of cta_phase_staged, of kScaledStages stages, each holding the
+// source lines and then the destination columns of its tile (with two
+// stages the wait is for all copies: the next tile's are issued after it).
 template <int THREADS, int TDS, int ES, int PATHS>
 __device__ __forceinline__ void cta_phase_staged_scaled(const PlanList &list,
                                                         unsigned char *smem) {
     constexpr int TD = 1 << TDS;
-    constexpr int S = kStages;
+    constexpr int S = kScaledStages;
     constexpr int SBS = StagedTile<2 * TD>::bytes;
     constexpr int SB = SBS + StagedDst<TD, ES>::bytes;
     const long long n = list.total_cta;
