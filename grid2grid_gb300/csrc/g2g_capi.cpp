@@ -518,7 +518,7 @@ void assemble(g2g_plan &pl) {
     pl.paths = 0;
     // every CTA-level tile a plain transpose of 4-byte (8-byte) elements;
     // every tile a scaled transpose of 4-byte (8-byte) elements
-    bool only_w4 = true, only_w8 = true, only_w4s = true, only_w8s = true;
+    bool only_w4 = true, only_w8 = true, only_w16 = true, only_w4s = true, only_w8s = true;
     for (int k = 0; k < pl.n_pairs; ++k) {
         PairHost &p = pl.host[k];
         g2g::PairInfo &pi = pl.pinfo[k];
@@ -609,6 +609,8 @@ void assemble(g2g_plan &pl) {
             only_w4 = false;
         if (p.cast || p.scaled || (p.any_trans && p.esz != 8))
             only_w8 = false;
+        if (p.cast || p.scaled || (p.any_trans && p.esz != 16))
+            only_w16 = false;
         if (!p.scaled || p.cast || any_plain || p.esz != 4)
             only_w4s = false;
         if (!p.scaled || p.cast || any_plain || p.esz != 8)
@@ -618,6 +620,8 @@ void assemble(g2g_plan &pl) {
         pl.paths |= 64;
     if (only_w8 && (pl.paths & 2))
         pl.paths |= 128;
+    if (only_w16 && (pl.paths & 2))
+        pl.paths |= 256;
     if (only_w4s && pl.n_pairs > 0)
         pl.paths |= 1024;
     if (only_w8s && pl.n_pairs > 0)
@@ -781,7 +785,7 @@ constexpr size_t kMaxSmemPerCta = 227 * 1024;
 // one element size, are its only tiles (bit 64 or 128 set, no copy tiles).
 bool uses_staged_ring(int paths) {
     return ((paths & ~(64 | 32)) == 2 && (paths & 64)) ||
-           ((paths & ~(128 | 32)) == 2 && (paths & 128));
+           ((paths & ~(128 | 32)) == 2 && (paths & 128)) || paths == (2 | 256);
 }
 // ... and the staged ring of scaled transposes when every tile is a scaled
 // transpose of one element size (bit 1024 or 2048 set).
@@ -807,7 +811,7 @@ g2g::ScatterConfig scatter_config(const g2g_plan &pl) {
     // narrow transposes only: their staged ring, unless the tuning asks for
     // the register path or blocks live in host memory
     if (pl.tuning.ring == -1 || pl.host_memory)
-        c.paths &= ~(64 | 128 | 1024 | 2048);
+        c.paths &= ~(64 | 128 | 256 | 1024 | 2048);
     if (uses_staged_ring(c.paths))
         c.smem_bytes = g2g::staged_transpose_smem_bytes(c.tile_dim);
     if (uses_staged_scaled_ring(c.paths))
@@ -868,7 +872,7 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
     long long tiles = 0;
     // bit 64 (128) holds for the launch when every plan with CTA-level tiles
     // has it, bit 1024 (2048) when every plan has it
-    bool w4 = true, w8 = true, w4s = true, w8s = true;
+    bool w4 = true, w8 = true, w16 = true, w4s = true, w8s = true;
     for (int k = 0; k < n; ++k) {
         const g2g::ScatterConfig ck = scatter_config(*plans[k]);
         if (plans[k]->host_memory) {
@@ -879,6 +883,8 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
             w4 = false;
         if ((ck.paths & (2 | 4 | 8 | 16)) && !(ck.paths & 128))
             w8 = false;
+        if ((ck.paths & (2 | 4 | 8 | 16)) && !(ck.paths & 256))
+            w16 = false;
         if (!(ck.paths & 1024))
             w4s = false;
         if (!(ck.paths & 2048))
@@ -887,8 +893,9 @@ g2g::ScatterConfig merged_config(g2g_plan *const *plans, int n) {
         c.trans_bytes = std::max(c.trans_bytes, ck.trans_bytes);
         tiles += plans[k]->n_tiles;
     }
-    c.paths = (c.paths & ~(64 | 128 | 1024 | 2048)) | (w4 && (c.paths & 2) ? 64 : 0) |
-              (w8 && (c.paths & 2) ? 128 : 0) | (w4s ? 1024 : 0) | (w8s ? 2048 : 0);
+    c.paths = (c.paths & ~(64 | 128 | 256 | 1024 | 2048)) | (w4 && (c.paths & 2) ? 64 : 0) |
+              (w8 && (c.paths & 2) ? 128 : 0) | (w16 && (c.paths & 2) ? 256 : 0) |
+              (w4s ? 1024 : 0) | (w8s ? 2048 : 0);
     c.smem_bytes = uses_staged_ring(c.paths) ? g2g::staged_transpose_smem_bytes(c.tile_dim)
                    : uses_staged_scaled_ring(c.paths)
                        ? g2g::staged_scaled_transpose_smem_bytes(c.tile_dim)
@@ -1536,7 +1543,7 @@ g2g_status g2g_plan_autotune(g2g_plan *plan, void *stream, int32_t iters, g2g_tu
                                         if (!(plan->paths & 1) &&
                                             (sg != -1 ||
                                              (rg != 1 &&
-                                              !(plan->paths & (64 | 128 | 1024 | 2048)))))
+                                              !(plan->paths & (64 | 128 | 256 | 1024 | 2048)))))
                                             continue;
                                         if (sg != -1 && rg != 1)
                                             continue;

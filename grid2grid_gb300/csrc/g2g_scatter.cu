@@ -119,6 +119,7 @@ cudaError_t preload_scatter_kernels() {
                              PATH_COPY | PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE,
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W4_STAGED,
                              PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W8_STAGED,
+                             PATH_TRANSPOSE | PATH_W16_STAGED,
                              PATH_COPY | PATH_SCALED_REAL, PATH_COPY | PATH_SCALED_COMPLEX,
                              PATH_COPY | PATH_CAST, PATH_SCALED_REAL | PATH_W4S_STAGED,
                              PATH_SCALED | PATH_W8S_STAGED};
@@ -135,7 +136,7 @@ cudaError_t preload_scatter_kernels() {
                     c.paths = paths;
                     c.tile_dim = 32;
                     c.trans_bytes = c.smem_bytes = transpose_smem_bytes(32, 16);
-                    if (paths & (PATH_W4_STAGED | PATH_W8_STAGED))
+                    if (paths & (PATH_W4_STAGED | PATH_W8_STAGED | PATH_W16_STAGED))
                         c.smem_bytes = staged_smem_bytes(32);
                     if (paths & (PATH_W4S_STAGED | PATH_W8S_STAGED))
                         c.smem_bytes = staged_scaled_smem_bytes(32);

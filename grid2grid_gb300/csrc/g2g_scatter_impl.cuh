@@ -64,6 +64,7 @@ enum : int {
     PATH_W4_STAGED = 64, // every CTA-level tile a plain transpose of 4-byte
                          // elements, staged raw through a cp.async ring
     PATH_W8_STAGED = 128, // the same for 8-byte elements
+    PATH_W16_STAGED = 256, // and for 16-byte ones (td x td tiles)
     PATH_W4S_STAGED = 1024, // every tile a scaled transposed tile of 4-byte
                             // elements: the ring stages their destination too
     PATH_W8S_STAGED = 2048  // the same for 8-byte elements
@@ -1941,6 +1942,110 @@ __device__ __forceinline__ void cta_phase_staged(const PlanList &list, unsigned 
     cp_async_wait<0>();
 }
 
+// Plain transposed tiles of 16-byte elements (td x td) on the same ring
+// (PATH_W16_STAGED): a source line of td elements, 16 td bytes at a phase of
+// at most 12, lies in td + 1 aligned blocks (td + 1 lanes a line, a pitch of
+// 4 (td + 1) words); a stage is smaller than the narrow ring's.
+template <int TD> struct StagedTile16 {
+    static constexpr int blocks = TD + 1;
+    static constexpr int pitch = 4 * blocks;
+    static constexpr int bytes = TD * pitch * 4;
+};
+template <int THREADS, int TD>
+__device__ __forceinline__ void staged_issue16(const Tile &t, uint32_t st) {
+    constexpr int G = StagedTile16<TD>::blocks;
+    constexpr int RSTEP = THREADS / G;
+    constexpr int NP = (TD + RSTEP - 1) / RSTEP;
+    constexpr int P = StagedTile16<TD>::pitch;
+    const int g = threadIdx.x % G;
+    const int r0 = threadIdx.x / G;
+    if (r0 >= RSTEP)
+        return;
+    const int run = t.cols * 16;
+    const int rel = g * 16;
+    uint64_t s = t.src + (uint64_t)((long long)r0 * t.src_ld);
+    const uint64_t sstep = (uint64_t)((long long)RSTEP * t.src_ld);
+    uint32_t d = st + (uint32_t)((r0 * P + 4 * g) * 4);
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const int ph = (int)(s & 15u);
+        if (r0 + i * RSTEP < t.rows && rel < ph + run)
+            cp_async16(d, s - (uint64_t)ph + (uint64_t)rel);
+        s += sstep;
+        d += (uint32_t)(RSTEP * P * 4);
+    }
+}
+// A thread per final row r, columns c0, c0 + CSTEP, ...; element c of line r
+// at words q_r + 4 c .. + 3. AL: every address and stride a multiple of 16
+// (one 16-byte read and store), else 4-byte words.
+template <int THREADS, int TD, bool AL>
+__device__ __forceinline__ void staged_store16(const Tile &t, const uint32_t *st) {
+    constexpr int CSTEP = THREADS / TD;
+    constexpr int NC = (TD + CSTEP - 1) / CSTEP;
+    constexpr int P = StagedTile16<TD>::pitch;
+    const int r = threadIdx.x % TD;
+    const int c0 = threadIdx.x / TD;
+    if (r >= t.rows)
+        return;
+    const uint64_t s = t.src + (uint64_t)((long long)r * t.src_ld);
+    const uint32_t *p = st + r * P + (int)((s & 15u) >> 2) + c0 * 4;
+    uint64_t a = t.dst + (uint64_t)((long long)c0 * t.dst_ld + (long long)r * 16);
+    const uint64_t step = (uint64_t)((long long)CSTEP * t.dst_ld);
+    // complex<double> 'C': the imaginary part's sign is its top word's
+    const uint32_t flip = (t.kind & KIND_CONJ) ? 0x80000000u : 0u;
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        if (c0 + i * CSTEP < t.cols) {
+            const uint32_t *e = p + i * CSTEP * 4;
+            if constexpr (AL) {
+                const uint4 v = *reinterpret_cast<const uint4 *>(e);
+                st_v4(a, make_uint4(v.x, v.y, v.z, v.w ^ flip));
+            } else {
+                st_u32(a, e[0]);
+                st_u32(a + 4, e[1]);
+                st_u32(a + 8, e[2]);
+                st_u32(a + 12, e[3] ^ flip);
+            }
+        }
+        a += step;
+    }
+}
+template <int THREADS, int TDS>
+__device__ __forceinline__ void cta_phase_staged16(const PlanList &list, unsigned char *smem) {
+    constexpr int TD = 1 << TDS;
+    constexpr int S = kStages;
+    constexpr int SB = StagedTile16<TD>::bytes;
+    const long long n = list.total_cta;
+    const long long G = gridDim.x;
+    const uint32_t base = smem_addr(smem);
+    const PairInfo *unused;
+#pragma unroll
+    for (int k = 0; k < S - 1; ++k) {
+        const long long ti = (long long)blockIdx.x + (long long)k * G;
+        if (ti < n)
+            staged_issue16<THREADS, TD>(*locate_cta(list, ti, unused), base + (uint32_t)(k * SB));
+        cp_async_commit();
+    }
+    int st = 0;
+    for (long long ti = blockIdx.x; ti < n; ti += G) {
+        cp_async_wait<S - 2>();
+        __syncthreads();
+        const long long nx = ti + (long long)(S - 1) * G;
+        const int sn = st == 0 ? S - 1 : st - 1;
+        if (nx < n)
+            staged_issue16<THREADS, TD>(*locate_cta(list, nx, unused), base + (uint32_t)(sn * SB));
+        cp_async_commit();
+        const Tile t = *locate_cta(list, ti, unused);
+        const uint32_t *stage = reinterpret_cast<const uint32_t *>(smem + st * SB);
+        if (elem_mode(t) == EM_16)
+            staged_store16<THREADS, TD, true>(t, stage);
+        else
+            staged_store16<THREADS, TD, false>(t, stage);
+        st = st + 1 == S ? 0 : st + 1;
+    }
+    cp_async_wait<0>();
+}
+
 // Scaled transposed tiles of one element size (4 or 8 bytes) when they are
 // the launch's only tiles (PATH_W4S_STAGED, PATH_W8S_STAGED): the ring stages
 // the source lines as above and, behind them in the same stage, the tile's
@@ -2103,6 +2208,10 @@ __device__ __forceinline__ void cta_phase_t(const PlanList &list, unsigned char 
     }
     if constexpr ((PATHS & PATH_W8_STAGED) != 0) {
         cta_phase_staged<THREADS, TDS, 8>(list, smem);
+        return;
+    }
+    if constexpr ((PATHS & PATH_W16_STAGED) != 0) {
+        cta_phase_staged16<THREADS, TDS>(list, smem);
         return;
     }
     if constexpr ((PATHS & PATH_W4S_STAGED) != 0) {
@@ -3090,6 +3199,8 @@ cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cuda
         (cfg.paths & PATH_W8_STAGED))
         return launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE | PATH_W8_STAGED>(
             l, cfg, s);
+    if (cfg.paths == (PATH_TRANSPOSE | PATH_W16_STAGED))
+        return launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_W16_STAGED>(l, cfg, s);
     const bool narrow = (cfg.paths & PATH_NARROW_TRANSPOSE) != 0;
     if ((cfg.paths & ~PATH_NARROW_TRANSPOSE) == PATH_TRANSPOSE)
         return narrow ? launch_u<THREADS, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)

@@ -137,7 +137,8 @@ typedef struct g2g_tuning {
     int32_t ring;             /* plain copies when not TMA-staged: 1 = per-warp
                                  cp.async ring in shared memory, -1 = loads
                                  through registers (0 = default). Launches of
-                                 plain 4- or 8-byte transposes only: 1 = their
+                                 transposes of one element size only (plain,
+                                 or scaled 4- or 8-byte ones): 1 = their
                                  staged cp.async ring, -1 = the register path */
     int32_t tile_run;         /* ring: a warp takes runs of this many
                                  consecutive tiles (1, 2, 4 .. 64; 0 = default) */
@@ -169,9 +170,10 @@ typedef struct g2g_plan_info {
     int32_t tile_paths;       /* tile kinds of the work list: 1 copy, 2 transpose,
                                  4 scaled real, 8 scaled complex, 16 cast,
                                  32 transposes of 4- or 8-byte elements,
-                                 64 / 128 transposes of 4- / 8-byte elements
-                                 only (they run on the staged cp.async ring
-                                 when no copy tiles come with them, the
+                                 64 / 128 / 256 transposes of 4- / 8- /
+                                 16-byte elements only (they run on the
+                                 staged cp.async ring when no copy tiles
+                                 come with them, the
                                  tuning's ring is not -1 and no block is in
                                  host memory), 1024 / 2048 scaled transposes
                                  of 4- / 8-byte elements only (their staged

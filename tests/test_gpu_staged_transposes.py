@@ -286,3 +286,33 @@ def test_scaled_transposes_batch_and_mixed():
         got2 = T.gpu_run(Li2, Lf2, ai2, af2, ops2, how="plan")
         for k in range(len(Li2)):
             T.assert_arenas_equal(got2[k], want2[k], Lf2[k], what=f"scaled mixed pair {k}")
+
+
+STAGED16 = 256
+
+
+@pytest.mark.parametrize("tuning", [None, dict(tile_dim=16), dict(threads=512), dict(ring=-1)])
+def test_complex_double_transposes_staged_match_port(tuning):
+    """complex<double> 'T' / 'C' (tile path 256) at 16-byte aligned addresses
+    (one 16-byte read and store per element), with blocks at 8-byte aligned
+    ones (4-byte words), and a block-cyclic pair."""
+    rng = np.random.default_rng(1030 + (0 if tuning is None else len(str(tuning))))
+    for t, (m, n), bm in (("T", (233, 301), (0, 0)), ("C", (300, 180), (0, 0)),
+                          ("T", (150, 211), (8, 0)), ("C", (211, 150), (0, 8)),
+                          ("T", (97, 131), (8, 8))):
+        Li, Lf, ai, af, op = _float_pair(rng, m, n, t, dt=capi.COMPLEX128, byte_mis=bm, ext_hi=70)
+        assert _staged(_tile_paths([Li], [Lf], [op]), STAGED16)
+        want = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+        for how in ("plan", "graph"):
+            got = T.gpu_run([Li], [Lf], [ai], [af], [op], how=how, tuning=tuning,
+                            executes=2)[0]
+            T.assert_arenas_equal(got, want, Lf, what=f"c128 {t} {bm} {how} {tuning}")
+    Li = Ls.scalapack_layout(512, 384, 64, 64, 2, 2, capi.COMPLEX128)
+    Lf = Ls.scalapack_layout(384, 512, 96, 40, 2, 2, capi.COMPLEX128)
+    ai = Ls.fill_random(np.zeros(Li.arena_bytes, np.uint8), rng)
+    af = Ls.fill_random(np.zeros(Lf.arena_bytes, np.uint8), rng)
+    op = ("T", 1.0, 0.0)
+    assert _staged(_tile_paths([Li], [Lf], [op]), STAGED16)
+    want = T.port_run([Li], [Lf], [ai], [af], [op])[0]
+    got = T.gpu_run([Li], [Lf], [ai], [af], [op], how="plan", tuning=tuning)[0]
+    T.assert_arenas_equal(got, want, Lf, what=f"c128 block-cyclic {tuning}")
