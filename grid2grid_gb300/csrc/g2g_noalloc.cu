@@ -19,8 +19,7 @@
 //    that overlap on the GPU race on the array: issue them one at a time per
 //    device (each call returns only after its transform has completed);
 //  * the first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress while that device is current; make that first call
-//    before any stream capture.
+//    cudaGetSymbolAddress while that device is current.
 #include "g2g_host.hpp"
 
 #include <cuda_runtime.h>

@@ -288,9 +288,8 @@ g2g_status g2g_transform_batch(int32_t n_pairs,
  * G2G_ERROR_OUT_OF_MEMORY before any device work; all calls share the array,
  * so calls that overlap on the GPU race (the call synchronises `stream` and
  * returns after its transform has completed; issue calls one at a time per
- * device). The first call on a device resolves the array's address; make it
- * before any stream capture. One dtype and op as in g2g_transform; `op` may
- * be NULL. */
+ * device). The first call on a device resolves the array's address. One
+ * dtype and op as in g2g_transform; `op` may be NULL. */
 g2g_status g2g_transform_noalloc(const g2g_layout_desc *initial,
                                  const g2g_layout_desc *final_, g2g_dtype dtype,
                                  const g2g_op *op, void *stream);
