@@ -3202,9 +3202,10 @@ cudaError_t launch_plain_paths(const PlanList &l, const ScatterConfig &cfg, cuda
     if (cfg.paths == (PATH_TRANSPOSE | PATH_W16_STAGED))
         return launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_W16_STAGED>(l, cfg, s);
     const bool narrow = (cfg.paths & PATH_NARROW_TRANSPOSE) != 0;
+    // (without copy tiles the unroll knob acts on nothing: one instance)
     if ((cfg.paths & ~PATH_NARROW_TRANSPOSE) == PATH_TRANSPOSE)
-        return narrow ? launch_u<THREADS, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)
-                      : launch_u<THREADS, PATH_TRANSPOSE>(l, cfg, s);
+        return narrow ? launch_t<THREADS, 1, PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)
+                      : launch_t<THREADS, 1, PATH_TRANSPOSE>(l, cfg, s);
     return narrow ? launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE | PATH_NARROW_TRANSPOSE>(l, cfg, s)
                   : launch_u<THREADS, PATH_COPY | PATH_TRANSPOSE>(l, cfg, s);
 }
